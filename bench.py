@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 workset assembly path on the 128^3 Q1 hex steady-thermal workload (C2).
+
+A step is one Jacobian+residual assembly (assembleJacRes with fused zero-fill) over all 2,097,152
+cells, inputs resident in HBM.  The L2 is flushed (256 MB write) before every timed step, outside the
+CUDA events that time the step.  Printed as one JSON line on rank 0.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference algorithm (the oracle; the reference
+itself cannot be built without Trilinos) on the host cores with all threads, each step a bounded
+sample of the same workload.  With N > 1 (torchrun) every rank runs an independent replica of the
+workload (the problem has no exchange step in this form), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = None
+try:
+    METRIC = json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"]
+except Exception:
+    METRIC = "Jac+res cells/s FP64 vs mixed (rel res<=1e-10); DOF/s; serve p50/p99 ms"
+
+WORKLOAD = ("C2: steady thermal, unit cube, 128^3 Q1 hex (2,097,152 cells, 8 nodes/cell, 2x2x2 Gauss), "
+            "kappa=exp(0.5 g) per cell, f=1, u=0 on x=0 and x=1, one Jacobian+residual assembly per step")
+
+
+def algorithmic_bytes(ncell, nnode, nnz, s_j, npe=8):
+    """Bytes one Q1 Jac+res assembly must move: J values, u and r, kappa and connectivity, coordinates."""
+    return nnz * s_j + nnode * (8 + 8) + ncell * (8 + 4 * npe) + nnode * 24
+
+
+def read_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def read_profile_traffic(name):
+    """traffic (bytes/launch) recorded from an ncu capture in profiles/<name>.md (line 'traffic_bytes_per_launch: X')."""
+    path = os.path.join(ROOT, "profiles", name + ".md")
+    try:
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        rows = []
+        for ts, line in self.lines:
+            if not (t0 <= ts <= t1):
+                continue
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(f[1]), smax=float(f[2]), power=float(f[3]) if f[3] not in ("[N/A]", "N/A") else 0.0,
+                                 hw=f[5], hwt=f[6], swt=f[7], swp=f[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        reasons = set()
+        for r in rows:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                              ("swp", "sw_power_cap")):
+                if r[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
+                "power_w_max": max(r["power"] for r in rows), "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(n=128, slab=64, seed=2, threads=None, reps=5):
+    """The oracle (C++ restatement of the reference algorithm, FP64 forward AD, OpenMP atomic scatter)
+    timed on the host cores on the first `slab` z-layers of C2: the first slab*n*n cells of the mesh
+    with their kappa (same cell size, same coefficient stream)."""
+    from mrhyde_gb300.workloads import lognormal_kappa
+    from oracle.oracle import OracleProblem, max_threads
+
+    threads = threads or max_threads()
+    kap = lognormal_kappa(n ** 3, seed, 0.5)[: slab * n * n]
+    P = OracleProblem(dim=3, order=1, n=(n, n, slab), lo=(0, 0, 0), hi=(1.0, 1.0, slab / n), kind=0,
+                      source=("const", 1.0, 0.0), kappa=kap, dirichlet_faces=3, workset_size=1024)
+    u = np.random.default_rng(7).uniform(-1, 1, P.ndof)
+    best = []
+    P.assemble(u, nthreads=threads)  # warm-up
+    for _ in range(reps):
+        t = time.perf_counter()
+        P.assemble(u, nthreads=threads)
+        best.append(time.perf_counter() - t)
+    dt = statistics.median(best)
+    return dict(value=P.ncell / dt, unit="cells/s", cores=threads, kind="port",
+                sample=f"first {slab} z-layers of C2 ({P.ncell} cells of 128^3, same kappa stream), "
+                       f"Jac+res with 8-tangent forward AD, OpenMP atomic scatter, median of {reps} after 1 warm-up",
+                seconds_per_sample=dt)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    n = 128
+    step_slab = 4
+    # K steps, each a bounded sample of the workload (first `step_slab` z-layers of C2)
+    from mrhyde_gb300.workloads import lognormal_kappa
+    from oracle.oracle import OracleProblem, max_threads
+
+    threads = max_threads()
+    kap = lognormal_kappa(n ** 3, 2, 0.5)[: step_slab * n * n]
+    P = OracleProblem(dim=3, order=1, n=(n, n, step_slab), hi=(1.0, 1.0, step_slab / n), kind=0, source=("const", 1.0, 0.0),
+                      kappa=kap, dirichlet_faces=3, workset_size=1024)
+    u = np.random.default_rng(7).uniform(-1, 1, P.ndof)
+    for _ in range(args.warmup):
+        P.assemble(u, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        P.assemble(u, nthreads=threads)
+    dt = time.perf_counter() - t0
+    value = P.ncell * args.steps / dt
+    out = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "sample_cells_per_step": P.ncell,
+                      "note": "reference (Trilinos/Kokkos) cannot be built here; timed: its algorithm restated in C++ (oracle/)"},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
+                            "sample": f"first {step_slab} z-layers of C2 per step ({P.ncell} cells)"},
+           "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import mrhyde_gb300
+    from mrhyde_gb300 import AssemblyManager, Problem, SolverManager
+    from mrhyde_gb300.workloads import c2
+
+    torch.cuda.set_device(local_rank)
+    mrhyde_gb300.load()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+    cfg = c2(seed=2 + rank, n=args.n)
+    P = Problem(**cfg)
+    A = AssemblyManager(P)
+    info = P.info
+    u = torch.tensor(np.random.default_rng(7 + rank).uniform(0.0, 1.0, info.n_dofs), device="cuda")
+    r = P.new_vector()
+    J64 = P.new_matrix_values(fp32=False)
+    J32 = P.new_matrix_values(fp32=True)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MB > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        barrier()
+        for k in range(steps):
+            flush.fill_(k)
+            ev[k][0].record(stream)
+            fn()
+            ev[k][1].record(stream)
+        barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        tot = sum(ms)
+        if dist:
+            t = torch.tensor([tot], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot, ms
+
+    jac64 = lambda: A.assembleJacRes(u, r, J64, overwrite=True)
+    jac32 = lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True)
+    res64 = lambda: A.assembleRes(u, r, overwrite=True)
+    for _ in range(max(args.warmup, 3)):
+        jac64(); jac32(); res64()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.6)
+    t_clock0 = time.time()
+    tot64, ms64 = timed(jac64, args.steps)
+    # keep the same work running ~1.5 s so that the clock record has samples under load
+    t_end = time.time() + 1.5
+    while time.time() < t_end:
+        for _ in range(50):
+            jac64()
+        torch.cuda.synchronize()
+    t_clock1 = time.time()
+    tot32, ms32 = timed(jac32, args.steps)
+    totres, _ = timed(res64, args.steps)
+
+    # e2e through the public API with host buffers: H2D u, assemble, D2H J and r, every step
+    u_h = torch.empty(info.n_dofs, dtype=torch.float64, pin_memory=True)
+    u_h.copy_(u.cpu())
+    J_h = torch.empty(info.nnz, dtype=torch.float64, pin_memory=True)
+    r_h = torch.empty(info.n_dofs, dtype=torch.float64, pin_memory=True)
+    ud = P.new_vector()
+
+    def e2e_step():
+        ud.copy_(u_h, non_blocking=True)
+        A.assembleJacRes(ud, r, J64, overwrite=True)
+        J_h.copy_(J64, non_blocking=True)
+        r_h.copy_(r, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    n_e2e = min(args.steps, 20)
+    tot_e2e, _ = timed(e2e_step, n_e2e)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.stop()
+
+    cells = info.n_cells
+    ms_step = tot64 / args.steps
+    value = world * cells * args.steps / (tot64 * 1e-3)
+    peaks, peak_kind = read_peaks()
+    algo64 = algorithmic_bytes(cells, info.n_dofs, info.nnz, 8)
+    algo32 = algorithmic_bytes(cells, info.n_dofs, info.nnz, 4)
+    ach64 = algo64 / (ms_step * 1e-3) / 1e9
+    traffic = read_profile_traffic("k_fact_hex_fp64_c2_128")
+    dp_ops = 73 * (info.n_dofs - info.n_fixed)  # FP64 instructions per launch (19 DADD + 27 DMUL + 27 DFMA per free row)
+    dp_peak = 0.507e12  # measured DFMA instructions/s on this GB300 (FP64 pipe), see profiles/fp64_pipe_gb300.md
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": cells, "dofs": info.n_dofs, "nnz": info.nnz,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed before every timed step (256 MB write, outside the step's CUDA events)",
+                   "path": "factored row-gather (kappa_c * K_ref, one CSR row per thread, smem-staged 16B stores)"},
+        "dof_per_s": world * info.n_dofs * args.steps / (tot64 * 1e-3),
+        "mixed": {"value": world * cells * args.steps / (tot32 * 1e-3), "unit": "cells/s",
+                  "ms_per_step": tot32 / args.steps, "dtype": "J f32 / residual f64",
+                  "speedup_vs_fp64": tot64 / tot32},
+        "residual_only": {"value": world * cells * args.steps / (totres * 1e-3), "unit": "cells/s",
+                          "ms_per_step": totres / args.steps},
+        "roofline": {"bound": "hbm", "achieved": ach64, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach64 / peaks["hbm_gbs"], "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": algo64,
+                     "fp64_pipe": {"dp_instr_per_launch": dp_ops, "achieved_dp_instr_per_s": dp_ops / (ms_step * 1e-3),
+                                   "peak_dp_instr_per_s": dp_peak, "frac": dp_ops / (ms_step * 1e-3) / dp_peak}},
+        "e2e": {"value": world * cells * n_e2e / (tot_e2e * 1e-3), "unit": "cells/s",
+                "h2d_bytes_per_step": info.n_dofs * 8, "d2h_bytes_per_step": info.nnz * 8 + info.n_dofs * 8},
+        "gpu_launches": args.steps,
+    }
+    out["mixed"]["roofline_frac"] = algo32 / (tot32 / args.steps * 1e-3) / 1e9 / peaks["hbm_gbs"]
+    if sampler:
+        out["clocks"] = sampler.summary(t_clock0, t_clock1)
+
+    # End-to-end solve: Newton (FP64 J + FP64 PCG) vs mixed (FP32 J + FP32 inner PCG, FP64 residual),
+    # both to relative residual 1e-10, same initial guess; states the mixed result's error vs FP64.
+    if not args.no_solve:
+        sol = {}
+        ref_u = None
+        for mode in ("fp64", "mixed"):
+            S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=12,
+                              linear_tol=1e-11 if mode == "fp64" else 1e-4, linear_maxiter=20000,
+                              mixed_precision=mode == "mixed")
+            uu = P.new_vector()
+            S.nonlinearSolver(uu)  # warm (allocates workspace, captures graphs)
+            uu.zero_()
+            barrier()
+            t = time.perf_counter()
+            res = S.nonlinearSolver(uu, raise_on_noconv=False)
+            barrier()
+            dt = time.perf_counter() - t
+            sol[mode] = {"seconds": dt, "cells_per_s": world * cells / dt, "newton_iters": res.outer_iterations,
+                         "pcg_iters": res.iterations, "rel_residual_inf": res.rel_residual}
+            if mode == "fp64":
+                ref_u = uu.clone()
+            else:
+                sol[mode]["max_rel_diff_vs_fp64"] = float((uu - ref_u).abs().max() / ref_u.abs().max())
+        sol["mixed_speedup_e2e"] = sol["fp64"]["seconds"] / sol["mixed"]["seconds"]
+        out["solve"] = sol
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline()
+        except Exception as e:  # reported, never fatal
+            out["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

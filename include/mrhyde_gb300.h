@@ -1,0 +1,184 @@
+/*
+ * mrhyde_gb300.h -- C ABI of the GB300-native (sm_103a) workset finite-element assembly path.
+ *
+ * The entry points replace, for one GPU, the calls MrHyDE's SolverManager makes into its
+ * AssemblyManager and its own Krylov loop (paths relative to the MrHyDE source tree):
+ *
+ *   mrg_problem_create    AssemblyManager ctor + createGroups + DiscretizationInterface setup +
+ *                         LinearAlgebraInterface::setupLinearAlgebra graph
+ *                         (src/managers/assembly/assemblyManager_construct.hpp:14-180,
+ *                          src/managers/assembly/assemblyManager_groups.hpp:14-286,
+ *                          src/interfaces/linear_algebra/linearAlgebraInterface_construct.hpp:214-265)
+ *   mrg_get_graph         the overlapped CrsGraph the scatter targets (getLocalMatrixDevice row_map/entries,
+ *                         src/managers/assembly/assemblyManager_jacres.hpp:145-151)
+ *   mrg_assemble          AssemblyManager::assembleJacRes / assembleRes
+ *                         (src/managers/assembly/assemblyManager.hpp:237-259, :330-380;
+ *                          body src/managers/assembly/assemblyManager_jacres.hpp:121-630, :669-880)
+ *   mrg_set_dirichlet     SolverManager::setDirichlet (src/managers/solver/solverManager_util.hpp:60-140)
+ *   mrg_spmv              Tpetra CrsMatrix::apply as used by SolverManager::PCG
+ *                         (src/managers/solver/solverManager_solvers.hpp:852, :884)
+ *   mrg_solve_pcg         SolverManager::PCG (src/managers/solver/solverManager_solvers.hpp:812-901)
+ *   mrg_newton            SolverManager::nonlinearSolver (src/managers/solver/solverManager_solvers.hpp:290-643)
+ *
+ * Contract (mirrors the reference's Tpetra contract, jacres:145-151 and solverManager_solvers.hpp:345-355):
+ *   - The caller owns u, r, the CSR arrays and the CSR values, all in device memory.
+ *   - Assembly ADDS INTO r and J ("sum-into", like CrsMatrix::sumIntoValues) unless MRG_ASM_OVERWRITE is
+ *     given, which is exactly "J.setAllToScalar(0); r.putScalar(0);" fused into the assembly.
+ *   - Dirichlet rows are not scattered; afterwards J(d,d) = 1 (replace), as setJacobianConstraints does.
+ *   - J values must be laid out on the graph returned by mrg_get_graph (canonical structured numbering,
+ *     sorted columns).
+ *   - All work is enqueued on the caller's stream; nothing synchronises the host except the calls that
+ *     return host-visible results (mrg_solve_pcg / mrg_newton statistics).
+ *   - Every call returns an mrg_status; no C++ exception crosses the ABI.  mrg_last_error() gives text.
+ *   - A handle is thread-compatible (one host thread at a time per handle).
+ */
+#ifndef MRHYDE_GB300_H
+#define MRHYDE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* mrg_stream_t; /* identical to cudaStream_t; NULL = legacy default stream */
+typedef struct mrg_problem mrg_problem;
+
+typedef enum mrg_status {
+  MRG_OK = 0,
+  MRG_EINVAL = 1,   /* bad argument (null pointer, size out of range, unsupported combination) */
+  MRG_ENOMEM = 2,   /* device allocation failed */
+  MRG_ECUDA = 3,    /* a CUDA runtime call failed */
+  MRG_ETIMEOUT = 4, /* a bounded device-side wait gave up */
+  MRG_ENOTSUP = 5,  /* feature of the reference not built here (adjoint, sensitivities, ...) */
+  MRG_ENOCONV = 6,  /* iterative solver did not reach its tolerance */
+  MRG_ENUMERIC = 7  /* NaN/Inf detected in input or iteration (e.g. non-SPD matrix in PCG) */
+} mrg_status;
+
+/* Physics forms (the reference's "thermal" module, src/physics/thermal.cpp:71-165). */
+enum {
+  MRG_THERMAL = 0,         /* -div(kappa_cell grad u) = f                    */
+  MRG_DIFFUSION_1PU2 = 1   /* -div((1 + u^2) grad u) = f, "thermal diffusion: 1+T^2" */
+};
+/* Source term forms ("thermal source" function). */
+enum { MRG_SRC_CONST = 0, MRG_SRC_SINPROD = 1 /* amp * prod_d sin(freq * x_d) */ };
+/* Dirichlet faces of the structured box. */
+enum {
+  MRG_FACE_XLO = 1, MRG_FACE_XHI = 2, MRG_FACE_YLO = 4, MRG_FACE_YHI = 8,
+  MRG_FACE_ZLO = 16, MRG_FACE_ZHI = 32, MRG_FACE_ALL = 63
+};
+/* Dirichlet value forms. */
+enum { MRG_DBC_CONST = 0, MRG_DBC_NODE = 1 /* per-DOF host array of length n_dofs */ };
+
+typedef struct mrg_mesh_desc {
+  int32_t dim;    /* 2 (quadrilaterals) or 3 (hexahedra) */
+  int32_t order;  /* Lagrange order, 1 or 2 (equispaced nodes, HGRAD_{QUAD,HEX}_C1 / _Cn) */
+  int32_t nx, ny, nz;
+  double lo[3], hi[3];
+  /* Optional host array [(nx+1)(ny+1)(nz+1) * dim] of vertex coordinates (x fastest).  NULL = uniform
+     box.  When given, cells may be non-affine and the exact per-cell AD path is used. */
+  const double* vertex_coords;
+} mrg_mesh_desc;
+
+typedef struct mrg_physics_desc {
+  int32_t kind;            /* MRG_THERMAL or MRG_DIFFUSION_1PU2 */
+  int32_t source_kind;     /* MRG_SRC_* */
+  double source_amp, source_freq;
+  double kappa_const;      /* used when kappa_cell is NULL */
+  const double* kappa_cell;/* optional host array [n_cells] */
+  uint32_t dirichlet_faces;/* MRG_FACE_* bitmask */
+  int32_t dirichlet_kind;  /* MRG_DBC_* */
+  double dirichlet_const;
+  const double* dirichlet_node; /* host [n_dofs], read at the fixed DOFs (MRG_DBC_NODE) */
+  int32_t quad_order;      /* 0 -> 2*order (discretizationInterface_construct.hpp:111) */
+  int32_t reserved;
+} mrg_physics_desc;
+
+typedef struct mrg_problem_info {
+  int64_t n_dofs, n_cells, nnz, n_fixed;
+  int32_t nodes_per_cell, qp_per_cell;
+  int32_t path;            /* MRG_PATH_* chosen at creation */
+  int32_t reserved;
+} mrg_problem_info;
+
+enum {
+  MRG_PATH_FACTORED = 1,   /* identical affine cells: K_e = kappa_c * K_ref, row-gather assembly */
+  MRG_PATH_CELL = 2,       /* per-cell geometry + forward-AD tangents in registers, colored scatter */
+  MRG_PATH_Q2_TC = 3       /* Q2 hexahedra: element contractions on tensor cores (tcgen05) */
+};
+
+/* mrg_assemble flags */
+enum {
+  MRG_ASM_RES = 1u,            /* residual r += -res.val()                       */
+  MRG_ASM_JAC = 2u,            /* Jacobian J += res.dx()                         */
+  MRG_ASM_J_FP32 = 4u,         /* J_vals is float[] (mixed precision), else double[] */
+  MRG_ASM_OVERWRITE = 8u,      /* fused J.setAllToScalar(0), r.putScalar(0)      */
+  MRG_ASM_FIX_ZERO_ROWS = 16u, /* "fix zero rows" (jacres:609-628)               */
+  MRG_ASM_FORCE_CELL = 256u,   /* force the per-cell AD path (testing)           */
+  MRG_ASM_ATOMIC = 512u,       /* per-cell path: atomic scatter instead of 8-colour scatter */
+  MRG_ASM_ADJOINT = 1024u,     /* not supported -> MRG_ENOTSUP                   */
+  MRG_ASM_SENS = 2048u         /* not supported -> MRG_ENOTSUP                   */
+};
+
+/* ---- problem lifetime ------------------------------------------------------------------------- */
+int mrg_problem_create(const mrg_mesh_desc* mesh, const mrg_physics_desc* phys, mrg_problem** out);
+int mrg_problem_destroy(mrg_problem* p);
+int mrg_problem_get_info(const mrg_problem* p, mrg_problem_info* info);
+
+/* ---- structure (device output buffers, enqueued on stream) ------------------------------------ */
+int mrg_get_graph(const mrg_problem* p, int64_t* row_ptr /*[n_dofs+1]*/, int32_t* col_idx /*[nnz]*/,
+                  mrg_stream_t stream);
+int mrg_get_dof_map(const mrg_problem* p, int32_t* lids /*[n_cells*nodes_per_cell]*/, mrg_stream_t stream);
+int mrg_get_fixed_dofs(const mrg_problem* p, int32_t* dofs /*[n_fixed]*/, double* values /*[n_fixed] or NULL*/,
+                       mrg_stream_t stream);
+
+/* ---- coefficients and Dirichlet data --------------------------------------------------------- */
+int mrg_set_kappa(mrg_problem* p, const double* kappa_dev /*[n_cells]*/, mrg_stream_t stream);
+int mrg_set_dirichlet(const mrg_problem* p, double* u_dev /*[n_dofs]*/, mrg_stream_t stream);
+
+/* ---- assembly -------------------------------------------------------------------------------- */
+int mrg_assemble(mrg_problem* p, const double* u_dev, double* r_dev, void* J_vals_dev, uint32_t flags,
+                 mrg_stream_t stream);
+
+/* ---- linear algebra on the assembled system -------------------------------------------------- */
+/* y = J x on the canonical graph; J_fp32 != 0 means J_vals is float[]. */
+int mrg_spmv(const mrg_problem* p, const void* J_vals_dev, int32_t J_fp32, const double* x_dev, double* y_dev,
+             mrg_stream_t stream);
+
+typedef struct mrg_solve_stats {
+  int32_t iterations;       /* PCG iterations (summed over refinement / Newton steps) */
+  int32_t outer_iterations; /* Newton / refinement iterations                        */
+  double rel_residual;      /* final ||r||_2/||r0||_2 (PCG) or ||F||_inf/||F0||_inf (Newton) */
+  double abs_residual;
+  int32_t status;           /* mrg_status of the solve                                */
+  int32_t reserved;
+} mrg_solve_stats;
+
+/* Jacobi PCG on J x = b (x holds the initial guess).  Same iteration and stopping test as the
+   reference (rel. 2-norm).  Synchronises `stream` once at the end to return stats. */
+int mrg_solve_pcg(mrg_problem* p, const void* J_vals_dev, int32_t J_fp32, const double* b_dev, double* x_dev,
+                  double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
+
+typedef struct mrg_newton_opts {
+  double nl_tol;        /* relative inf-norm tolerance ("nonlinear TOL")                       */
+  int32_t max_iters;    /* "max nonlinear iters"                                                */
+  int32_t mixed;        /* 1: FP32 Jacobian + FP32 inner PCG, FP64 residual and update          */
+  double lin_tol;       /* PCG relative tolerance (FP64 path) or inner tolerance (mixed path)   */
+  int32_t lin_maxiter;
+  int32_t reuse_jacobian; /* 1: assemble J once (linear problems)                              */
+} mrg_newton_opts;
+
+/* Newton on F(u) = 0 with u on device (holding the initial guess; Dirichlet values are set first).
+   Uses library-owned device workspace (allocated on first use, freed with the problem). */
+int mrg_newton(mrg_problem* p, double* u_dev, const mrg_newton_opts* opts, mrg_solve_stats* stats,
+               mrg_stream_t stream);
+
+/* ---- diagnostics ----------------------------------------------------------------------------- */
+int mrg_last_error(char* buf, size_t len);   /* copies the calling thread's last error message */
+const char* mrg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MRHYDE_GB300_H */

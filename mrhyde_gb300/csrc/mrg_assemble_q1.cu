@@ -1,0 +1,802 @@
+// Assembly kernels of the workset path (reference: src/managers/assembly/assemblyManager_jacres.hpp:121-630,
+// src/physics/thermal.cpp:71-165, src/managers/assembly/assemblyManager_scatter.hpp:164-278).
+//
+// Two ways to build the same J and r:
+//
+//  (1) Factored row-gather path (identical affine cells, thermal physics, kappa constant per cell).
+//      Every cell has K_e = kappa_c * K_ref, where K_ref is the Q1 stiffness of one box cell with
+//      kappa = 1 -- the reference's identical-element "basis database" reuse
+//      (src/managers/assembly/assemblyManager_database.hpp:12-80) taken to its end.  For a box, the
+//      entry K_ref[l(i)][l(j)] depends only on the offset class (|dx|,|dy|,|dz|) of the node pair, so
+//      the assembled entry is J(i, i+off) = K(|off|) * S(off) with S(off) the sum of kappa over the
+//      cells containing both nodes.  One thread owns one CSR row: it gathers the kappa of the 8 (4)
+//      cells around its node, forms all S(off) with 19 (5) separable additions, writes its row once
+//      and forms r_i = b_i - sum_off J(i,i+off) u(i+off).  Rows of one CTA are contiguous in CSR, so
+//      the CTA stages its segment in shared memory and writes it with 16-byte streaming stores.  No
+//      atomics, no column search, no zero-fill pass, every nonzero written exactly once.
+//
+//  (2) Per-cell path (any geometry; any physics form; Q1 or Q2).  One CTA slice per cell: one
+//      thread per quadrature point computes the geometric Jacobian from the cell vertices, the
+//      physical gradients and the fields at that point into shared memory; then one thread per
+//      element row i runs the reference's forward-AD residual literally -- res_i as a dual number with
+//      one tangent per element DOF, seeded e_j (src/tools/workset.cpp:884) -- and scatters -res.val
+//      into r and res.dx into its CSR row (slots computed analytically).  Cells are processed in
+//      2^dim colours so that no two cells of one launch share a node (non-atomic RMW), or in one
+//      launch with atomics (MRG_ASM_ATOMIC).
+#include <cstdio>
+
+#include "mrg_internal.h"
+
+namespace {
+
+constexpr int FT = 128;  // rows per CTA in the factored path
+
+__device__ __forceinline__ void decompose(const Grid& g, int64_t n, int& ix, int& iy, int& iz) {
+  ix = (int)(n % g.nn[0]);
+  int64_t t = n / g.nn[0];
+  iy = (int)(t % g.nn[1]);
+  iz = (int)(t / g.nn[1]);
+}
+
+__device__ __forceinline__ int64_t row_ptr_of(const Grid& g, int64_t n, int64_t nrows) {
+  if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
+  int ix, iy, iz;
+  decompose(g, n, ix, iy, iz);
+  int lo, cx, cy, cz;
+  axis_range(ix, g.nn[0], g.p, lo, cx);
+  axis_range(iy, g.nn[1], g.p, lo, cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, lo, cz); else cz = 1;
+  return g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+}
+
+// Copy (or add) a contiguous segment from shared memory to global memory.  src[k] <-> dst[k]; both
+// pointers have the same address phase modulo 16 bytes, so the body uses aligned 16-byte accesses.
+template <typename T, bool ADD>
+__device__ __forceinline__ void seg_store(T* __restrict__ dst, const T* __restrict__ src, int64_t len) {
+  constexpr int V = 16 / sizeof(T);
+  int head = (int)(((16 - ((uintptr_t)dst & 15)) & 15) / sizeof(T));
+  if (head > len) head = (int)len;
+  for (int k = threadIdx.x; k < head; k += blockDim.x) {
+    if (ADD) dst[k] += src[k]; else dst[k] = src[k];
+  }
+  int64_t body = (len - head) / V;
+  if constexpr (sizeof(T) == 8) {
+    const double2* s2 = reinterpret_cast<const double2*>(src + head);
+    double2* d2 = reinterpret_cast<double2*>(dst + head);
+    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) {
+      double2 x = s2[v];
+      if (ADD) { double2 y = d2[v]; x.x += y.x; x.y += y.y; d2[v] = x; } else __stcs(d2 + v, x);
+    }
+  } else {
+    const float4* s4 = reinterpret_cast<const float4*>(src + head);
+    float4* d4 = reinterpret_cast<float4*>(dst + head);
+    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) {
+      float4 x = s4[v];
+      if (ADD) { float4 y = d4[v]; x.x += y.x; x.y += y.y; x.z += y.z; x.w += y.w; d4[v] = x; } else __stcs(d4 + v, x);
+    }
+  }
+  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) {
+    if (ADD) dst[k] += src[k]; else dst[k] = src[k];
+  }
+}
+
+struct FactArgs {
+  Grid g;
+  double Kp[8];
+  float Kp32[8];
+  double load;        // f * int(phi_l) over one cell (constant source)
+  int src_sin;        // 1: b_i = amp * Bx[ix] * By[iy] (* Bz[iz])
+  double amp;
+  const double* B[3];
+  int64_t nrows, nnz;
+};
+
+// ------------------------------------------------------------------------------------------------
+// (1) factored row-gather, hexahedra.  JT = double (FP64 mode) or float (mixed mode).
+// ------------------------------------------------------------------------------------------------
+template <typename JT, bool DOJ, bool DOR, bool OVW>
+__global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double* __restrict__ u,
+                                                  const double* __restrict__ kap, const float* __restrict__ kap32,
+                                                  double* __restrict__ r, JT* __restrict__ J) {
+  constexpr bool MIXED = sizeof(JT) == 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Grid& g = A.g;
+  const int64_t n0 = (int64_t)blockIdx.x * FT;
+  const int64_t n = n0 + threadIdx.x;
+  const int64_t nend = (n0 + FT < A.nrows) ? n0 + FT : A.nrows;
+  const int64_t seg0 = row_ptr_of(g, n0, A.nrows);
+  const int64_t seg1 = row_ptr_of(g, nend, A.nrows);
+  // stage so that smem and global share the 16-byte phase
+  constexpr int V = 16 / sizeof(JT);
+  const int phase = DOJ ? (int)(((uintptr_t)(J + seg0) & 15) / sizeof(JT)) : 0;
+  JT* sv = reinterpret_cast<JT*>(smem_raw) + phase;
+
+  bool active = n < A.nrows;
+  bool fixed = false;
+  int64_t myrow = 0, diagpos = 0;
+  if (active) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    const int NX = g.nn[0], NY = g.nn[1], NZ = g.nn[2];
+    const int nx = g.nc[0], ny = g.nc[1], nz = g.nc[2];
+    int lo, cx, cy, cz;
+    axis_range(ix, NX, 1, lo, cx);
+    axis_range(iy, NY, 1, lo, cy);
+    axis_range(iz, NZ, 1, lo, cz);
+    myrow = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+    const int64_t loc = myrow - seg0;
+    fixed = node_fixed(g, ix, iy, iz);
+    const bool vx[3] = {ix > 0, true, ix < NX - 1};
+    const bool vy[3] = {iy > 0, true, iy < NY - 1};
+    const bool vz[3] = {iz > 0, true, iz < NZ - 1};
+    if (fixed) {
+      // row of a Dirichlet DOF: never scattered (scatter.hpp:208,253); diagonal set to 1 afterwards
+      if (DOJ) {
+        int pos = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+          for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx)
+              if (vz[dz + 1] && vy[dy + 1] && vx[dx + 1]) {
+                if (dx == 0 && dy == 0 && dz == 0) diagpos = pos;
+                sv[loc + pos] = (OVW && dx == 0 && dy == 0 && dz == 0) ? JT(1) : JT(0);
+                ++pos;
+              }
+      }
+      if (DOR && OVW) r[n] = 0.0;
+    } else {
+      // kappa of the 8 cells around the node (0 outside the mesh)
+      double k[2][2][2];
+      float k32[2][2][2];
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            int ccx = ix - 1 + a, ccy = iy - 1 + b, ccz = iz - 1 + c;
+            bool ok = ccx >= 0 && ccx < nx && ccy >= 0 && ccy < ny && ccz >= 0 && ccz < nz;
+            int64_t cid = ccx + (int64_t)nx * (ccy + (int64_t)ny * ccz);
+            k[c][b][a] = ok ? __ldg(kap + cid) : 0.0;
+            if (MIXED && DOJ) k32[c][b][a] = ok ? __ldg(kap32 + cid) : 0.0f;
+          }
+      // separable sums: S[dz][dy][dx] = sum of kappa over the cells shared by node and node+off
+      double sx[2][2][3], sxy[2][3][3], S[3][3][3];
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          sx[c][b][0] = k[c][b][0];
+          sx[c][b][1] = k[c][b][0] + k[c][b][1];
+          sx[c][b][2] = k[c][b][1];
+        }
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          sxy[c][0][x] = sx[c][0][x];
+          sxy[c][1][x] = sx[c][0][x] + sx[c][1][x];
+          sxy[c][2][x] = sx[c][1][x];
+        }
+#pragma unroll
+      for (int y = 0; y < 3; ++y)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          S[0][y][x] = sxy[0][y][x];
+          S[1][y][x] = sxy[0][y][x] + sxy[1][y][x];
+          S[2][y][x] = sxy[1][y][x];
+        }
+      float S32[3][3][3];
+      if (MIXED && DOJ) {
+        float tx[2][2][3], txy[2][3][3];
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int b = 0; b < 2; ++b) {
+            tx[c][b][0] = k32[c][b][0];
+            tx[c][b][1] = k32[c][b][0] + k32[c][b][1];
+            tx[c][b][2] = k32[c][b][1];
+          }
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int x = 0; x < 3; ++x) {
+            txy[c][0][x] = tx[c][0][x];
+            txy[c][1][x] = tx[c][0][x] + tx[c][1][x];
+            txy[c][2][x] = tx[c][1][x];
+          }
+#pragma unroll
+        for (int y = 0; y < 3; ++y)
+#pragma unroll
+          for (int x = 0; x < 3; ++x) {
+            S32[0][y][x] = txy[0][y][x];
+            S32[1][y][x] = txy[0][y][x] + txy[1][y][x];
+            S32[2][y][x] = txy[1][y][x];
+          }
+      }
+      // load vector entry b_i
+      double b;
+      if (A.src_sin) b = A.amp * A.B[0][ix] * A.B[1][iy] * A.B[2][iz];
+      else b = A.load * (double)((cx == 3 ? 2 : 1) * (cy == 3 ? 2 : 1) * (cz == 3 ? 2 : 1));
+      double acc = b;
+      double t[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) t[c] = 0.0;
+      int pos = 0;
+      const int64_t plane = (int64_t)NX * NY;
+#pragma unroll
+      for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx)
+            if (vz[dz + 1] && vy[dy + 1] && vx[dx + 1]) {
+              const int cls = (dx != 0) + 2 * (dy != 0) + 4 * (dz != 0);
+              const double s = S[dz + 1][dy + 1][dx + 1];
+              if (!MIXED) {
+                const double a = A.Kp[cls] * s;
+                if (DOJ) sv[loc + pos] = (JT)a;
+                if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+              } else {
+                if (DOJ) sv[loc + pos] = (JT)(A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1]);
+                if (DOR) t[cls] = fma(s, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), t[cls]);
+              }
+              ++pos;
+            }
+      if (DOR) {
+        if (MIXED) {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) acc = fma(-A.Kp[c], t[c], acc);
+        }
+        if (OVW) r[n] = acc; else r[n] += acc;
+      }
+    }
+  }
+  if (DOJ) {
+    __syncthreads();
+    seg_store<JT, !OVW>(J + seg0, sv, seg1 - seg0);
+    if (!OVW) {
+      __syncthreads();
+      if (active && fixed) J[myrow + diagpos] = JT(1);
+    }
+  }
+  (void)V;
+}
+
+// ------------------------------------------------------------------------------------------------
+// (1') factored row-gather, quadrilaterals (2-D): 4 cells, 9 couplings per interior row.
+// ------------------------------------------------------------------------------------------------
+template <typename JT, bool DOJ, bool DOR, bool OVW>
+__global__ void __launch_bounds__(FT) k_fact_quad(const FactArgs A, const double* __restrict__ u,
+                                                   const double* __restrict__ kap, const float* __restrict__ kap32,
+                                                   double* __restrict__ r, JT* __restrict__ J) {
+  constexpr bool MIXED = sizeof(JT) == 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Grid& g = A.g;
+  const int64_t n0 = (int64_t)blockIdx.x * FT;
+  const int64_t n = n0 + threadIdx.x;
+  const int64_t nend = (n0 + FT < A.nrows) ? n0 + FT : A.nrows;
+  const int64_t seg0 = row_ptr_of(g, n0, A.nrows);
+  const int64_t seg1 = row_ptr_of(g, nend, A.nrows);
+  const int phase = DOJ ? (int)(((uintptr_t)(J + seg0) & 15) / sizeof(JT)) : 0;
+  JT* sv = reinterpret_cast<JT*>(smem_raw) + phase;
+  bool active = n < A.nrows, fixed = false;
+  int64_t myrow = 0, diagpos = 0;
+  if (active) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    const int NX = g.nn[0], NY = g.nn[1];
+    const int nx = g.nc[0], ny = g.nc[1];
+    int lo, cx, cy;
+    axis_range(ix, NX, 1, lo, cx);
+    axis_range(iy, NY, 1, lo, cy);
+    myrow = g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix];
+    const int64_t loc = myrow - seg0;
+    fixed = node_fixed(g, ix, iy, 0);
+    const bool vx[3] = {ix > 0, true, ix < NX - 1};
+    const bool vy[3] = {iy > 0, true, iy < NY - 1};
+    if (fixed) {
+      if (DOJ) {
+        int pos = 0;
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx)
+            if (vy[dy + 1] && vx[dx + 1]) {
+              if (dx == 0 && dy == 0) diagpos = pos;
+              sv[loc + pos] = (OVW && dx == 0 && dy == 0) ? JT(1) : JT(0);
+              ++pos;
+            }
+      }
+      if (DOR && OVW) r[n] = 0.0;
+    } else {
+      double k[2][2];
+      float k32[2][2];
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          int ccx = ix - 1 + a, ccy = iy - 1 + b;
+          bool ok = ccx >= 0 && ccx < nx && ccy >= 0 && ccy < ny;
+          int64_t cid = ccx + (int64_t)nx * ccy;
+          k[b][a] = ok ? __ldg(kap + cid) : 0.0;
+          if (MIXED && DOJ) k32[b][a] = ok ? __ldg(kap32 + cid) : 0.0f;
+        }
+      double sx[2][3], S[3][3];
+      float S32[3][3];
+#pragma unroll
+      for (int b = 0; b < 2; ++b) { sx[b][0] = k[b][0]; sx[b][1] = k[b][0] + k[b][1]; sx[b][2] = k[b][1]; }
+#pragma unroll
+      for (int x = 0; x < 3; ++x) { S[0][x] = sx[0][x]; S[1][x] = sx[0][x] + sx[1][x]; S[2][x] = sx[1][x]; }
+      if (MIXED && DOJ) {
+        float tx[2][3];
+#pragma unroll
+        for (int b = 0; b < 2; ++b) { tx[b][0] = k32[b][0]; tx[b][1] = k32[b][0] + k32[b][1]; tx[b][2] = k32[b][1]; }
+#pragma unroll
+        for (int x = 0; x < 3; ++x) { S32[0][x] = tx[0][x]; S32[1][x] = tx[0][x] + tx[1][x]; S32[2][x] = tx[1][x]; }
+      }
+      double b;
+      if (A.src_sin) b = A.amp * A.B[0][ix] * A.B[1][iy];
+      else b = A.load * (double)((cx == 3 ? 2 : 1) * (cy == 3 ? 2 : 1));
+      double acc = b, t[4] = {0.0, 0.0, 0.0, 0.0};
+      int pos = 0;
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx)
+          if (vy[dy + 1] && vx[dx + 1]) {
+            const int cls = (dx != 0) + 2 * (dy != 0);
+            const double s = S[dy + 1][dx + 1];
+            if (!MIXED) {
+              const double a = A.Kp[cls] * s;
+              if (DOJ) sv[loc + pos] = (JT)a;
+              if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy), acc);
+            } else {
+              if (DOJ) sv[loc + pos] = (JT)(A.Kp32[cls] * S32[dy + 1][dx + 1]);
+              if (DOR) t[cls] = fma(s, __ldg(u + n + dx + (int64_t)NX * dy), t[cls]);
+            }
+            ++pos;
+          }
+      if (DOR) {
+        if (MIXED) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc = fma(-A.Kp[c], t[c], acc);
+        }
+        if (OVW) r[n] = acc; else r[n] += acc;
+      }
+    }
+  }
+  if (DOJ) {
+    __syncthreads();
+    seg_store<JT, !OVW>(J + seg0, sv, seg1 - seg0);
+    if (!OVW) {
+      __syncthreads();
+      if (active && fixed) J[myrow + diagpos] = JT(1);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// (2) per-cell path with forward-AD tangents in registers
+// ------------------------------------------------------------------------------------------------
+template <int N>
+struct Dual {
+  double v;
+  double d[N];
+};
+
+struct CellArgs {
+  Grid g;
+  QTab tab;
+  const double* vcoord;
+  int npe, nq, nvpe;
+  int kind, src_sin;
+  double amp, freq;
+  int color;        // -1: all cells (atomic scatter)
+  int cc[3];        // cells of this colour per axis
+  int64_t ncells_launch;
+};
+
+__device__ __forceinline__ void add_to(double* p, double v, bool atomic) {
+  if (atomic) atomicAdd(p, v); else *p += v;
+}
+__device__ __forceinline__ void add_to(float* p, float v, bool atomic) {
+  if (atomic) atomicAdd(p, v); else *p += v;
+}
+
+// DIM, P (order), NPE = (P+1)^DIM, NQ quadrature points, CPB cells per CTA (NPE threads per cell).
+template <int DIM, int P, int NQ, int CPB, typename JT, bool DOJ, bool DOR, bool ATOMIC>
+__global__ void __launch_bounds__(CPB*(P + 1) * (P + 1) * (DIM == 3 ? P + 1 : 1))
+    k_cell(const CellArgs A, const double* __restrict__ u, const double* __restrict__ kap, double* __restrict__ r,
+           JT* __restrict__ J) {
+  constexpr int NPE = (P + 1) * (P + 1) * (DIM == 3 ? P + 1 : 1);
+  constexpr int NV = (DIM == 3) ? 8 : 4;
+  __shared__ double s_gp[CPB][NQ][NPE][DIM];  // physical basis gradients
+  __shared__ double s_w[CPB][NQ];             // w * |detJ|
+  __shared__ double s_T[CPB][NQ];             // u_h at qp
+  __shared__ double s_dT[CPB][NQ][DIM];       // grad u_h at qp
+  __shared__ double s_f[CPB][NQ];             // source at qp
+  __shared__ double s_u[CPB][NPE];
+  __shared__ double s_x[CPB][NV][DIM];
+  __shared__ int32_t s_lid[CPB][NPE];
+  const int slot = threadIdx.x / NPE;  // cell within CTA
+  const int t = threadIdx.x % NPE;
+  const int64_t cl = (int64_t)blockIdx.x * CPB + slot;
+  const bool active = cl < A.ncells_launch;
+  const Grid& g = A.g;
+  int cx = 0, cy = 0, cz = 0;
+  if (active) {
+    if (A.color < 0) {
+      cx = (int)(cl % g.nc[0]);
+      int64_t tt = cl / g.nc[0];
+      cy = (int)(tt % g.nc[1]);
+      cz = (int)(tt / g.nc[1]);
+    } else {
+      int kx = (int)(cl % A.cc[0]);
+      int64_t tt = cl / A.cc[0];
+      int ky = (int)(tt % A.cc[1]);
+      int kz = (int)(tt / A.cc[1]);
+      cx = 2 * kx + (A.color & 1);
+      cy = 2 * ky + ((A.color >> 1) & 1);
+      cz = 2 * kz + ((A.color >> 2) & 1);
+    }
+    // gather (gather.hpp:224-232): DOF values and vertex coordinates of the cell
+    {
+      const int q1 = P + 1;
+      int a = t % q1, b = (t / q1) % q1, c = (DIM == 3) ? t / (q1 * q1) : 0;
+      int32_t lid = (P * cx + a) + g.nn[0] * ((P * cy + b) + g.nn[1] * (P * cz + c));
+      s_lid[slot][t] = lid;
+      s_u[slot][t] = __ldg(u + lid);
+    }
+    for (int v = t; v < NV; v += NPE) {
+      int a = v % 2, b = (v / 2) % 2, c = (DIM == 3) ? v / 4 : 0;
+      int64_t vid = (cx + a) + (int64_t)(g.nc[0] + 1) * ((cy + b) + (int64_t)(g.nc[1] + 1) * (cz + c));
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) s_x[slot][v][k] = __ldg(A.vcoord + vid * DIM + k);
+    }
+  }
+  __syncthreads();
+  // geometry and fields at the quadrature points (basis.hpp:407-455, integration.hpp:248-262,
+  // workset.cpp:1093-1105)
+  if (active) {
+    for (int q = t; q < NQ; q += NPE) {
+      double Jm[DIM][DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k)
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) Jm[k][m] = 0.0;
+      double xq[DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) xq[k] = 0.0;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double ps = A.tab.psi[v * NQ + q];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          xq[k] += s_x[slot][v][k] * ps;
+#pragma unroll
+          for (int m = 0; m < DIM; ++m) Jm[k][m] += s_x[slot][v][k] * A.tab.dpsi[(v * NQ + q) * DIM + m];
+        }
+      }
+      double det, Ji[DIM][DIM];
+      if constexpr (DIM == 2) {
+        det = Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0];
+        Ji[0][0] = Jm[1][1] / det; Ji[0][1] = -Jm[0][1] / det;
+        Ji[1][0] = -Jm[1][0] / det; Ji[1][1] = Jm[0][0] / det;
+      } else {
+        det = Jm[0][0] * (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) -
+              Jm[0][1] * (Jm[1][0] * Jm[2][2] - Jm[1][2] * Jm[2][0]) +
+              Jm[0][2] * (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]);
+        Ji[0][0] = (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) / det;
+        Ji[0][1] = (Jm[0][2] * Jm[2][1] - Jm[0][1] * Jm[2][2]) / det;
+        Ji[0][2] = (Jm[0][1] * Jm[1][2] - Jm[0][2] * Jm[1][1]) / det;
+        Ji[1][0] = (Jm[1][2] * Jm[2][0] - Jm[1][0] * Jm[2][2]) / det;
+        Ji[1][1] = (Jm[0][0] * Jm[2][2] - Jm[0][2] * Jm[2][0]) / det;
+        Ji[1][2] = (Jm[0][2] * Jm[1][0] - Jm[0][0] * Jm[1][2]) / det;
+        Ji[2][0] = (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]) / det;
+        Ji[2][1] = (Jm[0][1] * Jm[2][0] - Jm[0][0] * Jm[2][1]) / det;
+        Ji[2][2] = (Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0]) / det;
+      }
+      s_w[slot][q] = A.tab.w[q] * fabs(det);
+      double T = 0.0, dT[DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) dT[k] = 0.0;
+      for (int i = 0; i < NPE; ++i) {
+        double gp[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          double s = 0.0;
+#pragma unroll
+          for (int m = 0; m < DIM; ++m) s += Ji[m][k] * A.tab.dphi[(i * NQ + q) * DIM + m];
+          gp[k] = s;
+          s_gp[slot][q][i][k] = s;
+        }
+        const double ui = s_u[slot][i];
+        T += ui * A.tab.phi[i * NQ + q];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) dT[k] += ui * gp[k];
+      }
+      s_T[slot][q] = T;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) s_dT[slot][q][k] = dT[k];
+      double f = A.amp;
+      if (A.src_sin) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) f *= sin(A.freq * xq[k]);
+      }
+      s_f[slot][q] = f;
+    }
+  }
+  __syncthreads();
+  if (!active) return;
+  // forward-AD residual of row t (thermal.cpp:125-137); tangents seeded e_j (workset.cpp:884):
+  // dT/du_j = phi_j(q), d(grad T)/du_j = grad phi_j(q)
+  const int64_t cid = cx + (int64_t)g.nc[0] * (cy + (int64_t)g.nc[1] * cz);
+  const double kc = (A.kind == MRG_THERMAL) ? __ldg(kap + cid) : 0.0;
+  Dual<NPE> res;
+  res.v = 0.0;
+#pragma unroll
+  for (int j = 0; j < NPE; ++j) res.d[j] = 0.0;
+  for (int q = 0; q < NQ; ++q) {
+    const double w = s_w[slot][q];
+    const double phi_i = A.tab.phi[t * NQ + q];
+    res.v += (0.0 - s_f[slot][q]) * w * phi_i;
+    // diff = kappa_c (constant) or 1 + T^2 (dual)
+    Dual<NPE> diff;
+    if (A.kind == MRG_THERMAL) {
+      diff.v = kc;
+#pragma unroll
+      for (int j = 0; j < NPE; ++j) diff.d[j] = 0.0;
+    } else {
+      const double T = s_T[slot][q];
+      diff.v = 1.0 + T * T;
+#pragma unroll
+      for (int j = 0; j < NPE; ++j) diff.d[j] = 2.0 * T * A.tab.phi[j * NQ + q];
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      // (diff * dT_k) * w * grad_k phi_t, all as dual arithmetic
+      const double dTk = s_dT[slot][q][k];
+      const double gik = s_gp[slot][q][t][k];
+      const double sc = w * gik;
+      res.v += diff.v * dTk * sc;
+#pragma unroll
+      for (int j = 0; j < NPE; ++j) res.d[j] += (diff.d[j] * dTk + diff.v * s_gp[slot][q][j][k]) * sc;
+    }
+  }
+  // scatter (scatter.hpp:196-277): r += -res.val, J(row, cols) += res.dx; fixed rows skipped
+  const int32_t row = s_lid[slot][t];
+  const int q1 = P + 1;
+  int rx = P * cx + t % q1, ry = P * cy + (t / q1) % q1, rz = (DIM == 3) ? P * cz + t / (q1 * q1) : 0;
+  if (node_fixed(g, rx, ry, rz)) return;
+  if (DOR) add_to(r + row, -res.v, ATOMIC);
+  if (DOJ) {
+    int lx, ly, lz, nx_, ny_, nz_;
+    axis_range(rx, g.nn[0], P, lx, nx_);
+    axis_range(ry, g.nn[1], P, ly, ny_);
+    if (DIM == 3) axis_range(rz, g.nn[2], P, lz, nz_); else { lz = 0; nz_ = 1; }
+    const int64_t rp = g.P[2][rz] * g.T[1] * g.T[0] + (int64_t)nz_ * (g.P[1][ry] * g.T[0] + (int64_t)ny_ * g.P[0][rx]);
+#pragma unroll
+    for (int j = 0; j < NPE; ++j) {
+      int jx = P * cx + j % q1, jy = P * cy + (j / q1) % q1, jz = (DIM == 3) ? P * cz + j / (q1 * q1) : 0;
+      int64_t s = rp + ((int64_t)(jz - lz) * ny_ + (jy - ly)) * nx_ + (jx - lx);
+      add_to(J + s, (JT)res.d[j], ATOMIC);
+    }
+  }
+}
+
+__global__ void k_constraints_d(Grid g, const int32_t* __restrict__ fixed, int64_t n, double* __restrict__ J) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int d = fixed[k];
+  int ix, iy, iz;
+  decompose(g, d, ix, iy, iz);
+  int lx, ly, lz, cx, cy, cz;
+  axis_range(ix, g.nn[0], g.p, lx, cx);
+  axis_range(iy, g.nn[1], g.p, ly, cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, lz, cz); else { lz = 0; cz = 1; }
+  int64_t rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+  J[rp + ((int64_t)(iz - lz) * cy + (iy - ly)) * cx + (ix - lx)] = 1.0;
+}
+__global__ void k_constraints_f(Grid g, const int32_t* __restrict__ fixed, int64_t n, float* __restrict__ J) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int d = fixed[k];
+  int ix, iy, iz;
+  decompose(g, d, ix, iy, iz);
+  int lx, ly, lz, cx, cy, cz;
+  axis_range(ix, g.nn[0], g.p, lx, cx);
+  axis_range(iy, g.nn[1], g.p, ly, cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, lz, cz); else { lz = 0; cz = 1; }
+  int64_t rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+  J[rp + ((int64_t)(iz - lz) * cy + (iy - ly)) * cx + (ix - lx)] = 1.0f;
+}
+
+template <typename JT>
+__global__ void k_fix_zero_rows(Grid g, int64_t nrows, JT* __restrict__ J) {
+  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nrows) return;
+  int ix, iy, iz;
+  decompose(g, n, ix, iy, iz);
+  int lx, ly, lz, cx, cy, cz;
+  axis_range(ix, g.nn[0], g.p, lx, cx);
+  axis_range(iy, g.nn[1], g.p, ly, cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, lz, cz); else { lz = 0; cz = 1; }
+  int64_t rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+  int64_t len = (int64_t)cx * cy * cz;
+  double s = 0.0;
+  for (int64_t k = 0; k < len; ++k) s += fabs((double)J[rp + k]);
+  if (s < 1.0e-14) J[rp + ((int64_t)(iz - lz) * cy + (iy - ly)) * cx + (ix - lx)] = JT(1);
+}
+
+__global__ void k_kappa32(const double* __restrict__ k, float* __restrict__ k32, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) k32[i] = (float)k[i];
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <typename JT, bool DOJ, bool DOR, bool OVW>
+cudaError_t launch_fact(const mrg_problem* p, const FactArgs& A, const double* u, double* r, JT* J, cudaStream_t s) {
+  const int smem = DOJ ? (FT * (p->g.dim == 3 ? 27 : 9) + 16 / (int)sizeof(JT)) * (int)sizeof(JT) : 0;
+  const unsigned grid = nblk(p->ndof, FT);
+  if (p->g.dim == 3) {
+    auto kern = k_fact_hex<JT, DOJ, DOR, OVW>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
+  } else {
+    auto kern = k_fact_quad<JT, DOJ, DOR, OVW>;
+    kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
+  }
+  return cudaGetLastError();
+}
+
+template <typename JT>
+cudaError_t dispatch_fact(const mrg_problem* p, const FactArgs& A, const double* u, double* r, JT* J, bool doJ,
+                          bool doR, bool ovw, cudaStream_t s) {
+  if (doJ && doR) return ovw ? launch_fact<JT, true, true, true>(p, A, u, r, J, s) : launch_fact<JT, true, true, false>(p, A, u, r, J, s);
+  if (doJ) return ovw ? launch_fact<JT, true, false, true>(p, A, u, r, J, s) : launch_fact<JT, true, false, false>(p, A, u, r, J, s);
+  return ovw ? launch_fact<JT, false, true, true>(p, A, u, r, J, s) : launch_fact<JT, false, true, false>(p, A, u, r, J, s);
+}
+
+template <int DIM, int P, int NQ, int CPB, typename JT, bool DOJ, bool DOR, bool ATOMIC>
+cudaError_t launch_cell_t(const mrg_problem* p, CellArgs A, const double* u, double* r, JT* J, cudaStream_t s) {
+  constexpr int NPE = (P + 1) * (P + 1) * (DIM == 3 ? P + 1 : 1);
+  const Grid& g = p->g;
+  if (ATOMIC) {
+    A.color = -1;
+    A.ncells_launch = p->ncell;
+    k_cell<DIM, P, NQ, CPB, JT, DOJ, DOR, ATOMIC><<<nblk(A.ncells_launch, CPB), CPB * NPE, 0, s>>>(A, u, p->d_kappa, r, J);
+    return cudaGetLastError();
+  }
+  const int ncol = (DIM == 3) ? 8 : 4;
+  for (int c = 0; c < ncol; ++c) {
+    A.color = c;
+    int64_t tot = 1;
+    for (int k = 0; k < 3; ++k) {
+      int bit = (c >> k) & 1;
+      int nck = (k < DIM) ? g.nc[k] : 1;
+      A.cc[k] = (k < DIM) ? (nck - bit + 1) / 2 : 1;
+      if (k >= DIM && bit) A.cc[k] = 0;
+      tot *= A.cc[k];
+    }
+    A.ncells_launch = tot;
+    if (tot == 0) continue;
+    k_cell<DIM, P, NQ, CPB, JT, DOJ, DOR, false><<<nblk(tot, CPB), CPB * NPE, 0, s>>>(A, u, p->d_kappa, r, J);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <int DIM, int P, int NQ, int CPB, typename JT>
+cudaError_t launch_cell_flags(const mrg_problem* p, const CellArgs& A, const double* u, double* r, JT* J, bool doJ,
+                              bool doR, bool atomic, cudaStream_t s) {
+  if (atomic) {
+    if (doJ && doR) return launch_cell_t<DIM, P, NQ, CPB, JT, true, true, true>(p, A, u, r, J, s);
+    if (doJ) return launch_cell_t<DIM, P, NQ, CPB, JT, true, false, true>(p, A, u, r, J, s);
+    return launch_cell_t<DIM, P, NQ, CPB, JT, false, true, true>(p, A, u, r, J, s);
+  }
+  if (doJ && doR) return launch_cell_t<DIM, P, NQ, CPB, JT, true, true, false>(p, A, u, r, J, s);
+  if (doJ) return launch_cell_t<DIM, P, NQ, CPB, JT, true, false, false>(p, A, u, r, J, s);
+  return launch_cell_t<DIM, P, NQ, CPB, JT, false, true, false>(p, A, u, r, J, s);
+}
+
+}  // namespace
+
+int mrg_launch_factored(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s) {
+  FactArgs A;
+  A.g = p->g;
+  for (int c = 0; c < 8; ++c) {
+    A.Kp[c] = p->Kp[c];
+    A.Kp32[c] = (float)p->Kp[c];
+  }
+  A.src_sin = (p->source_kind == MRG_SRC_SINPROD);
+  A.amp = p->source_amp;
+  A.load = p->source_amp * p->cell_load;
+  if (A.src_sin) {
+    A.B[0] = p->d_srcB;
+    A.B[1] = p->d_srcB + p->g.nn[0];
+    A.B[2] = p->d_srcB + p->g.nn[0] + p->g.nn[1];
+  } else {
+    A.B[0] = A.B[1] = A.B[2] = nullptr;
+  }
+  A.nrows = p->ndof;
+  A.nnz = p->nnz;
+  const bool doJ = flags & MRG_ASM_JAC, doR = flags & MRG_ASM_RES, ovw = flags & MRG_ASM_OVERWRITE;
+  cudaError_t e;
+  if (flags & MRG_ASM_J_FP32) e = dispatch_fact<float>(p, A, u, r, (float*)J, doJ, doR, ovw, s);
+  else e = dispatch_fact<double>(p, A, u, r, (double*)J, doJ, doR, ovw, s);
+  if (e != cudaSuccess) return mrg_cuda_check(e, "factored assembly launch");
+  return MRG_OK;
+}
+
+int mrg_launch_cell(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s) {
+  CellArgs A;
+  A.g = p->g;
+  const int d = p->g.dim, npe = p->npe, nq = p->nq, nv = (d == 3) ? 8 : 4;
+  A.tab.w = p->d_qtab;
+  A.tab.phi = A.tab.w + nq;
+  A.tab.dphi = A.tab.phi + npe * nq;
+  A.tab.psi = A.tab.dphi + npe * nq * d;
+  A.tab.dpsi = A.tab.psi + nv * nq;
+  A.vcoord = p->d_vcoord;
+  A.npe = npe;
+  A.nq = nq;
+  A.nvpe = nv;
+  A.kind = p->kind;
+  A.src_sin = (p->source_kind == MRG_SRC_SINPROD);
+  A.amp = p->source_amp;
+  A.freq = p->source_freq;
+  A.color = -1;
+  A.cc[0] = A.cc[1] = A.cc[2] = 1;
+  A.ncells_launch = p->ncell;
+  const bool doJ = (flags & MRG_ASM_JAC) && J, doR = (flags & MRG_ASM_RES) && r, atomic = flags & MRG_ASM_ATOMIC;
+  const bool fp32 = flags & MRG_ASM_J_FP32;
+  cudaError_t e = cudaErrorInvalidValue;
+  const int p_ = p->g.p;
+  const int qo = p->quad_order;
+  // supported (dim, order, points per axis) combinations
+  const int n1 = qo / 2 + 1;
+  bool ok = true;
+#define MRG_CELL_CASE(DIM_, P_, N1_, CPB_)                                                                          \
+  else if (d == DIM_ && p_ == P_ && n1 == N1_) {                                                                    \
+    constexpr int NQ_ = N1_ * N1_ * (DIM_ == 3 ? N1_ : 1);                                                          \
+    if (fp32) e = launch_cell_flags<DIM_, P_, NQ_, CPB_, float>(p, A, u, r, (float*)J, doJ, doR, atomic, s);       \
+    else e = launch_cell_flags<DIM_, P_, NQ_, CPB_, double>(p, A, u, r, (double*)J, doJ, doR, atomic, s);          \
+  }
+  if (false) {
+  }
+  MRG_CELL_CASE(2, 1, 2, 32)
+  MRG_CELL_CASE(3, 1, 2, 16)
+  MRG_CELL_CASE(2, 2, 3, 8)
+  MRG_CELL_CASE(3, 2, 3, 2)
+  else ok = false;
+#undef MRG_CELL_CASE
+  if (!ok) return mrg_fail(MRG_ENOTSUP, "per-cell path: unsupported (dim, order, quadrature) combination");
+  if (e != cudaSuccess) return mrg_cuda_check(e, "per-cell assembly launch");
+  return MRG_OK;
+}
+
+int mrg_launch_constraints(mrg_problem* p, void* J, bool fp32, cudaStream_t s) {
+  if (p->nfixed == 0) return MRG_OK;
+  if (fp32) k_constraints_f<<<nblk(p->nfixed, 256), 256, 0, s>>>(p->g, p->d_fixed, p->nfixed, (float*)J);
+  else k_constraints_d<<<nblk(p->nfixed, 256), 256, 0, s>>>(p->g, p->d_fixed, p->nfixed, (double*)J);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "constraints launch");
+}
+
+int mrg_launch_fix_zero_rows(mrg_problem* p, void* J, bool fp32, cudaStream_t s) {
+  if (fp32) k_fix_zero_rows<float><<<nblk(p->ndof, 256), 256, 0, s>>>(p->g, p->ndof, (float*)J);
+  else k_fix_zero_rows<double><<<nblk(p->ndof, 256), 256, 0, s>>>(p->g, p->ndof, (double*)J);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "fix-zero-rows launch");
+}
+
+int mrg_launch_kappa32(mrg_problem* p, cudaStream_t s) {
+  k_kappa32<<<nblk(p->ncell, 256), 256, 0, s>>>(p->d_kappa, p->d_kappa32, p->ncell);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "kappa32 launch");
+}

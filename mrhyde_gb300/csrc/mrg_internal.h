@@ -1,0 +1,121 @@
+// Internal declarations shared by the translation units of libmrhyde_gb.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mrhyde_gb300.h"
+
+// ------------------------------------------------------------------------------------------------
+// Error plumbing: every C entry point returns an mrg_status; the message is kept per host thread.
+// ------------------------------------------------------------------------------------------------
+void mrg_set_error(const std::string& msg);
+int mrg_fail(int status, const std::string& msg);
+int mrg_cuda_check(cudaError_t e, const char* what);
+
+#define MRG_CUDA(call)                                          \
+  do {                                                          \
+    cudaError_t e__ = (call);                                   \
+    if (e__ != cudaSuccess) return mrg_cuda_check(e__, #call);  \
+  } while (0)
+
+// ------------------------------------------------------------------------------------------------
+// Structured grid description passed by value to kernels.
+//
+// Nodes of the (p*nx+1) x (p*ny+1) x (p*nz+1) grid are numbered ix + NX*(iy + NY*iz); cells
+// cx + nx*(cy + ny*cz); local node (a,b,c) -> a + (p+1)*(b + (p+1)*c).  The CSR graph is the union
+// of element couplings with sorted columns, so along every axis a row couples to a contiguous node
+// range [lo, lo+cnt) and the row length is the product of the three per-axis counts.  Rows are
+// ordered (iz, iy, ix), which gives
+//     row_ptr(ix,iy,iz) = Pz[iz]*Ty*Tx + cz(iz)*(Py[iy]*Tx + cy(iy)*Px[ix])
+// with P*[i] the per-axis prefix sums of the counts and T* their totals.
+// ------------------------------------------------------------------------------------------------
+struct Grid {
+  int dim, p;
+  int nc[3];       // cells per axis (nc[2] = 1 in 2-D)
+  int nn[3];       // nodes per axis (nn[2] = 1 in 2-D)
+  uint32_t faces;  // Dirichlet face mask
+  int64_t T[3];    // per-axis totals of the coupling counts
+  const int64_t* P[3];  // device per-axis prefix tables, length nn[k]+1
+};
+
+// Coupled node range along one axis for node index i (host + device).
+__host__ __device__ inline void axis_range(int i, int nnodes, int p, int& lo, int& cnt) {
+  int ncell = (nnodes - 1) / p;
+  int cf, cl;
+  if (i % p == 0) { cf = i / p - 1; cl = i / p; } else { cf = cl = i / p; }
+  if (cf < 0) cf = 0;
+  if (cl > ncell - 1) cl = ncell - 1;
+  lo = p * cf;
+  cnt = p * (cl - cf) + p + 1;
+}
+
+// Number of cells adjacent to node i along one axis (1 or 2) and the first one.
+__host__ __device__ inline void axis_cells(int i, int nnodes, int p, int& cf, int& ncells) {
+  int ncell = (nnodes - 1) / p;
+  int cl;
+  if (i % p == 0) { cf = i / p - 1; cl = i / p; } else { cf = cl = i / p; }
+  if (cf < 0) cf = 0;
+  if (cl > ncell - 1) cl = ncell - 1;
+  ncells = cl - cf + 1;
+}
+
+__host__ __device__ inline bool node_fixed(const Grid& g, int ix, int iy, int iz) {
+  uint32_t f = g.faces;
+  bool on = ((f & 1u) && ix == 0) || ((f & 2u) && ix == g.nn[0] - 1) || ((f & 4u) && iy == 0) ||
+            ((f & 8u) && iy == g.nn[1] - 1);
+  if (g.dim == 3) on = on || ((f & 16u) && iz == 0) || ((f & 32u) && iz == g.nn[2] - 1);
+  return on;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Problem handle.
+// ------------------------------------------------------------------------------------------------
+struct SolverWork;  // mrg_solver.cu
+
+struct mrg_problem {
+  Grid g;
+  int npe, nq, quad_order;
+  int64_t ndof, ncell, nnz, nfixed;
+  int path;
+  int kind, source_kind;
+  double source_amp, source_freq;
+  double lo[3], hi[3], h[3];
+  bool affine;                 // uniform box cells (no vertex_coords)
+  // device data owned by the handle
+  int64_t* d_prefix = nullptr;  // concatenated per-axis prefix tables
+  double* d_kappa = nullptr;    // [ncell]
+  float* d_kappa32 = nullptr;   // [ncell] FP32 copy for the mixed-precision Jacobian
+  int32_t* d_fixed = nullptr;   // [nfixed] fixed DOFs, increasing
+  double* d_fixed_vals = nullptr;
+  double* d_vcoord = nullptr;   // [nvert*dim] (general geometry) or null
+  double* d_srcB = nullptr;     // per-axis source tables (factored path, sinprod source)
+  double* d_qtab = nullptr;     // reference tables for the per-cell path: w, phi, dphi (+ geometric psi, dpsi)
+  // host copies of small tables
+  double Kp[8];                 // factored path: K(|dx|,|dy|,|dz|) of one cell, kappa = 1
+  double cell_load;             // factored path: int_cell phi_l for one node (vol / 2^dim)
+  std::vector<double> qtab_host;
+  SolverWork* work = nullptr;
+};
+
+// Layout of d_qtab for the per-cell path: [nq] weights, [npe*nq] phi, [npe*nq*dim] dphi,
+// [nvpe*nq] psi, [nvpe*nq*dim] dpsi.
+struct QTab {
+  const double* w;
+  const double* phi;
+  const double* dphi;
+  const double* psi;
+  const double* dpsi;
+};
+
+// Launchers (mrg_assemble_q1.cu)
+int mrg_launch_factored(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s);
+int mrg_launch_cell(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s);
+int mrg_launch_constraints(mrg_problem* p, void* J, bool fp32, cudaStream_t s);
+int mrg_launch_fix_zero_rows(mrg_problem* p, void* J, bool fp32, cudaStream_t s);
+int mrg_launch_kappa32(mrg_problem* p, cudaStream_t s);
+// Solver (mrg_solver.cu)
+void mrg_solver_free(mrg_problem* p);

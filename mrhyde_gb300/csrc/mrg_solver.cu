@@ -1,0 +1,772 @@
+// Linear algebra on the assembled system and the Newton driver.
+//
+//   mrg_spmv       y = J x on the canonical structured graph (Tpetra CrsMatrix::apply)
+//   mrg_solve_pcg  Jacobi PCG, the iteration of SolverManager::PCG
+//                  (src/managers/solver/solverManager_solvers.hpp:812-901)
+//   mrg_newton     SolverManager::nonlinearSolver (src/managers/solver/solverManager_solvers.hpp:290-643)
+//
+// Design: the column indices of the canonical graph are implied by the structured layout, so the
+// SpMV reads only the values (8 or 4 bytes per nonzero) and the source vector.  Every PCG iteration
+// is three kernels (SpMV+dot, vector update+dots, direction update); each dot product is reduced
+// deterministically by the "last block finishes the sum" pattern (partials written per block, a
+// counter incremented after a fence, the last block sums the partials in index order) -- no extra
+// launch, no spinning, and bit-identical results from run to run and independent of what else runs
+// on the GPU.  The scalars (alpha, beta, rho, norms, iteration count, done flag) live in device
+// memory, so a chunk of iterations is captured once as a CUDA graph and replayed; the host reads the
+// done flag once per chunk.  After convergence every kernel returns at entry.
+//
+// Mixed precision: the Jacobian values and the inner PCG vectors are FP32 (half the bytes per
+// iteration), dot products are accumulated in FP64 per block; the Newton residual, the update of u
+// and the stopping test stay FP64, so Newton / iterative refinement recovers the FP64 solution.
+#include <cmath>
+#include <vector>
+
+#include "mrg_internal.h"
+
+namespace {
+
+constexpr int ST = 128;          // rows per CTA
+constexpr int CHUNK = 16;        // PCG iterations per captured graph
+
+// device scalars of one PCG instance
+struct PcgScal {
+  double rho, rho_old, pq, alpha, beta, r0, rnorm, tol;
+  int iter, maxiter, done, status;
+  unsigned int counter;
+  int pad;
+};
+
+__device__ __forceinline__ void decompose(const Grid& g, int64_t n, int& ix, int& iy, int& iz) {
+  ix = (int)(n % g.nn[0]);
+  int64_t t = n / g.nn[0];
+  iy = (int)(t % g.nn[1]);
+  iz = (int)(t / g.nn[1]);
+}
+
+struct RowInfo {
+  int lx, ly, lz, cx, cy, cz;
+  int64_t rp;
+};
+
+__device__ __forceinline__ RowInfo row_info(const Grid& g, int ix, int iy, int iz) {
+  RowInfo R;
+  axis_range(ix, g.nn[0], g.p, R.lx, R.cx);
+  axis_range(iy, g.nn[1], g.p, R.ly, R.cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
+  R.rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)R.cz * (g.P[1][iy] * g.T[0] + (int64_t)R.cy * g.P[0][ix]);
+  return R;
+}
+
+// sum of v over the block, returned in thread 0 (FP64)
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sh[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ double block_max(double v) {
+  __shared__ double sh[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = fmax(s, sh[i]);
+  __syncthreads();
+  return s;
+}
+
+// Last-block reduction: each block stores its partials; the block that increments the counter last
+// sums all partials in index order (deterministic) and runs `fin`.  Returns true in that block.
+template <int K>
+__device__ __forceinline__ bool last_block(double* parts, const double (&mine)[K], unsigned int* counter) {
+  __shared__ bool amlast;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) parts[(size_t)k * gridDim.x + blockIdx.x] = mine[k];
+    __threadfence();
+    unsigned int prev = atomicAdd(counter, 1u);
+    amlast = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  return amlast;
+}
+
+template <int K>
+__device__ __forceinline__ void sum_parts(const double* parts, double (&out)[K], unsigned int* counter) {
+  // whole block cooperates; fixed order: thread t sums indices t, t+blockDim, ...; then tree by warp
+  for (int k = 0; k < K; ++k) {
+    double s = 0.0;
+    for (unsigned int i = threadIdx.x; i < gridDim.x; i += blockDim.x) s += ((volatile const double*)parts)[(size_t)k * gridDim.x + i];
+    s = block_sum(s);
+    out[k] = s;  // valid in thread 0
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// ------------------------------------------------------------------------------------------------
+// row kernels: y_i = sum_j J_ij x_j over the row of node i
+// ------------------------------------------------------------------------------------------------
+template <int P, typename JT, typename XT>
+__device__ __forceinline__ double row_apply(const Grid& g, const RowInfo& R, const JT* __restrict__ vals,
+                                            const XT* __restrict__ x) {
+  constexpr int MC = 2 * P + 1;
+  const int64_t NX = g.nn[0], plane = (int64_t)g.nn[0] * g.nn[1];
+  double acc = 0.0;
+  int pos = 0;
+#pragma unroll
+  for (int z = 0; z < (P == 1 ? 3 : MC); ++z) {
+    if (z < R.cz) {
+#pragma unroll
+      for (int y = 0; y < MC; ++y) {
+        if (y < R.cy) {
+          const int64_t base = (R.lx) + NX * (R.ly + y) + plane * (R.lz + z);
+#pragma unroll
+          for (int xo = 0; xo < MC; ++xo)
+            if (xo < R.cx) {
+              acc = fma((double)vals[pos], (double)__ldg(x + base + xo), acc);
+              ++pos;
+            }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// FP32 variant accumulating in FP32 (inner solve of the mixed path)
+template <int P>
+__device__ __forceinline__ float row_apply_f(const Grid& g, const RowInfo& R, const float* __restrict__ vals,
+                                             const float* __restrict__ x) {
+  constexpr int MC = 2 * P + 1;
+  const int64_t NX = g.nn[0], plane = (int64_t)g.nn[0] * g.nn[1];
+  float acc = 0.0f;
+  int pos = 0;
+#pragma unroll
+  for (int z = 0; z < MC; ++z) {
+    if (z < R.cz) {
+#pragma unroll
+      for (int y = 0; y < MC; ++y) {
+        if (y < R.cy) {
+          const int64_t base = (R.lx) + NX * (R.ly + y) + plane * (R.lz + z);
+#pragma unroll
+          for (int xo = 0; xo < MC; ++xo)
+            if (xo < R.cx) {
+              acc = fmaf(vals[pos], __ldg(x + base + xo), acc);
+              ++pos;
+            }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+template <int P, typename JT>
+__global__ void __launch_bounds__(ST) k_spmv(Grid g, int64_t nrows, const JT* __restrict__ J, const double* __restrict__ x,
+                                             double* __restrict__ y) {
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  if (n >= nrows) return;
+  int ix, iy, iz;
+  decompose(g, n, ix, iy, iz);
+  RowInfo R = row_info(g, ix, iy, iz);
+  y[n] = row_apply<P, JT, double>(g, R, J + R.rp, x);
+}
+
+// ---- FP64 PCG kernels ---------------------------------------------------------------------------
+struct PcgVec64 {
+  double *x, *r, *z, *p, *q, *minv, *parts;
+  const double* b;
+  const double* J;
+  PcgScal* s;
+};
+
+// r = b - J x, minv = 1/diag, z = minv r, p = z; partial r.r, r.z
+template <int P>
+__global__ void __launch_bounds__(ST) k_pcg64_init(Grid g, int64_t nrows, PcgVec64 V) {
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  double rr = 0.0, rz = 0.0;
+  if (n < nrows) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    RowInfo R = row_info(g, ix, iy, iz);
+    double ax = row_apply<P, double, double>(g, R, V.J + R.rp, V.x);
+    double d = V.J[R.rp + ((int64_t)(iz - R.lz) * R.cy + (iy - R.ly)) * R.cx + (ix - R.lx)];
+    double mi = 1.0 / d;
+    double r = V.b[n] - ax;
+    double z = r * mi;
+    V.minv[n] = mi;
+    V.r[n] = r;
+    V.z[n] = z;
+    V.p[n] = z;
+    rr = r * r;
+    rz = r * z;
+  }
+  double m[2] = {block_sum(rr), block_sum(rz)};
+  if (last_block<2>(V.parts, m, &V.s->counter)) {
+    double t[2];
+    sum_parts<2>(V.parts, t, &V.s->counter);
+    if (threadIdx.x == 0) {
+      PcgScal* s = V.s;
+      s->r0 = sqrt(t[0]);
+      s->rnorm = s->r0;
+      s->rho = t[1];
+      s->iter = 0;
+      s->status = MRG_OK;
+      s->done = (s->r0 == 0.0 || !(s->r0 / s->r0 > s->tol) || s->maxiter <= 0) ? 1 : 0;
+      if (!isfinite(s->r0)) { s->done = 1; s->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+// q = J p ; pq partial ; last block: alpha = rho / pq
+template <int P>
+__global__ void __launch_bounds__(ST) k_pcg64_spmv(Grid g, int64_t nrows, PcgVec64 V) {
+  if (((volatile PcgScal*)V.s)->done) return;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  double pq = 0.0;
+  if (n < nrows) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    RowInfo R = row_info(g, ix, iy, iz);
+    double q = row_apply<P, double, double>(g, R, V.J + R.rp, V.p);
+    V.q[n] = q;
+    pq = V.p[n] * q;
+  }
+  double m[1] = {block_sum(pq)};
+  if (last_block<1>(V.parts, m, &V.s->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.s->counter);
+    if (threadIdx.x == 0) {
+      PcgScal* s = V.s;
+      s->pq = t[0];
+      s->alpha = s->rho / t[0];
+      if (!(t[0] > 0.0) || !isfinite(s->alpha)) { s->status = MRG_ENUMERIC; s->done = 1; }
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha q ; z = minv r ; partial r.r, r.z ; last block: beta, stopping test
+__global__ void __launch_bounds__(ST) k_pcg64_update(int64_t nrows, PcgVec64 V) {
+  if (((volatile PcgScal*)V.s)->done) return;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  const double alpha = V.s->alpha;
+  double rr = 0.0, rz = 0.0;
+  if (n < nrows) {
+    V.x[n] = fma(alpha, V.p[n], V.x[n]);
+    double r = fma(-alpha, V.q[n], V.r[n]);
+    double z = r * V.minv[n];
+    V.r[n] = r;
+    V.z[n] = z;
+    rr = r * r;
+    rz = r * z;
+  }
+  double m[2] = {block_sum(rr), block_sum(rz)};
+  if (last_block<2>(V.parts, m, &V.s->counter)) {
+    double t[2];
+    sum_parts<2>(V.parts, t, &V.s->counter);
+    if (threadIdx.x == 0) {
+      PcgScal* s = V.s;
+      s->rnorm = sqrt(t[0]);
+      s->rho_old = s->rho;
+      s->rho = t[1];
+      s->beta = s->rho / s->rho_old;
+      s->iter += 1;
+      if (!(s->rnorm / s->r0 > s->tol) || s->iter >= s->maxiter) s->done = 1;
+      if (!isfinite(s->rnorm)) { s->done = 1; s->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(ST) k_pcg64_dir(int64_t nrows, PcgVec64 V) {
+  if (((volatile PcgScal*)V.s)->done) return;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  if (n < nrows) V.p[n] = fma(V.s->beta, V.p[n], V.z[n]);
+}
+
+// ---- FP32 inner PCG kernels (mixed path) ---------------------------------------------------------
+struct PcgVec32 {
+  float *x, *r, *z, *p, *q, *minv;
+  double* parts;
+  const double* b;   // FP64 right-hand side (converted on the fly)
+  const float* J;
+  PcgScal* s;
+};
+
+template <int P>
+__global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec32 V) {
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  double rr = 0.0, rz = 0.0;
+  if (n < nrows) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    RowInfo R = row_info(g, ix, iy, iz);
+    float d = V.J[R.rp + ((int64_t)(iz - R.lz) * R.cy + (iy - R.ly)) * R.cx + (ix - R.lx)];
+    float mi = 1.0f / d;
+    float r = (float)V.b[n];   // x0 = 0
+    float z = r * mi;
+    V.x[n] = 0.0f;
+    V.minv[n] = mi;
+    V.r[n] = r;
+    V.z[n] = z;
+    V.p[n] = z;
+    rr = (double)(r * r);
+    rz = (double)(r * z);
+  }
+  double m[2] = {block_sum(rr), block_sum(rz)};
+  if (last_block<2>(V.parts, m, &V.s->counter)) {
+    double t[2];
+    sum_parts<2>(V.parts, t, &V.s->counter);
+    if (threadIdx.x == 0) {
+      PcgScal* s = V.s;
+      s->r0 = sqrt(t[0]);
+      s->rnorm = s->r0;
+      s->rho = t[1];
+      s->iter = 0;
+      s->status = MRG_OK;
+      s->done = (s->r0 == 0.0 || s->maxiter <= 0) ? 1 : 0;
+      if (!isfinite(s->r0)) { s->done = 1; s->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(ST) k_pcg32_spmv(Grid g, int64_t nrows, PcgVec32 V) {
+  if (((volatile PcgScal*)V.s)->done) return;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  float pq = 0.0f;
+  if (n < nrows) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    RowInfo R = row_info(g, ix, iy, iz);
+    float q = row_apply_f<P>(g, R, V.J + R.rp, V.p);
+    V.q[n] = q;
+    pq = V.p[n] * q;
+  }
+  double m[1] = {block_sum((double)pq)};
+  if (last_block<1>(V.parts, m, &V.s->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.s->counter);
+    if (threadIdx.x == 0) {
+      PcgScal* s = V.s;
+      s->pq = t[0];
+      s->alpha = s->rho / t[0];
+      if (!(t[0] > 0.0) || !isfinite(s->alpha)) { s->status = MRG_ENUMERIC; s->done = 1; }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) {
+  if (((volatile PcgScal*)V.s)->done) return;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  const float alpha = (float)V.s->alpha;
+  float rr = 0.0f, rz = 0.0f;
+  if (n < nrows) {
+    V.x[n] = fmaf(alpha, V.p[n], V.x[n]);
+    float r = fmaf(-alpha, V.q[n], V.r[n]);
+    float z = r * V.minv[n];
+    V.r[n] = r;
+    V.z[n] = z;
+    rr = r * r;
+    rz = r * z;
+  }
+  double m[2] = {block_sum((double)rr), block_sum((double)rz)};
+  if (last_block<2>(V.parts, m, &V.s->counter)) {
+    double t[2];
+    sum_parts<2>(V.parts, t, &V.s->counter);
+    if (threadIdx.x == 0) {
+      PcgScal* s = V.s;
+      s->rnorm = sqrt(t[0]);
+      s->rho_old = s->rho;
+      s->rho = t[1];
+      s->beta = s->rho / s->rho_old;
+      s->iter += 1;
+      if (!(s->rnorm / s->r0 > s->tol) || s->iter >= s->maxiter) s->done = 1;
+      if (!isfinite(s->rnorm)) { s->done = 1; s->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(ST) k_pcg32_dir(int64_t nrows, PcgVec32 V) {
+  if (((volatile PcgScal*)V.s)->done) return;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  if (n < nrows) V.p[n] = fmaf((float)V.s->beta, V.p[n], V.z[n]);
+}
+
+// u += (double) du32   (mixed path update; Dirichlet rows have du = 0 because r = 0 there)
+__global__ void k_add_f32(int64_t n, const float* __restrict__ du, double* __restrict__ u) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) u[i] += (double)du[i];
+}
+__global__ void k_axpy(int64_t n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = fma(a, x[i], y[i]);
+}
+__global__ void k_f32_to_f64(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+
+// inf-norm with the last-block pattern; result in s->rnorm
+__global__ void __launch_bounds__(ST) k_norminf(int64_t n, const double* __restrict__ v, double* parts, PcgScal* s) {
+  int64_t i = (int64_t)blockIdx.x * ST + threadIdx.x;
+  double a = (i < n) ? fabs(v[i]) : 0.0;
+  if (i < n && !isfinite(v[i])) a = INFINITY;
+  double m[1] = {block_max(a)};
+  if (last_block<1>(parts, m, &s->counter)) {
+    double mx = 0.0;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) mx = fmax(mx, ((volatile double*)parts)[k]);
+    mx = block_max(mx);
+    if (threadIdx.x == 0) {
+      s->rnorm = mx;
+      s->counter = 0u;
+    }
+  }
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// workspace
+// ------------------------------------------------------------------------------------------------
+struct SolverWork {
+  int64_t n = 0, nnz = 0;
+  double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *minv = nullptr, *parts = nullptr;
+  float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr, *minv32 = nullptr;
+  PcgScal* s = nullptr;
+  PcgScal* h_s = nullptr;       // pinned host mirror
+  // Newton buffers
+  double *F = nullptr, *du = nullptr, *J64 = nullptr;
+  float* J32 = nullptr;
+  // captured iteration chunks
+  cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+  const void* g64_key[3] = {nullptr, nullptr, nullptr};
+  const void* g32_key[3] = {nullptr, nullptr, nullptr};
+  cudaStream_t g64_stream = nullptr, g32_stream = nullptr;
+};
+
+void mrg_solver_free(mrg_problem* p) {
+  SolverWork* w = p->work;
+  if (!w) return;
+  if (w->g64) cudaGraphExecDestroy(w->g64);
+  if (w->g32) cudaGraphExecDestroy(w->g32);
+  cudaFree(w->r); cudaFree(w->z); cudaFree(w->p); cudaFree(w->q); cudaFree(w->minv); cudaFree(w->parts);
+  cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->z32); cudaFree(w->p32); cudaFree(w->q32); cudaFree(w->minv32);
+  cudaFree(w->s);
+  if (w->h_s) cudaFreeHost(w->h_s);
+  cudaFree(w->F); cudaFree(w->du); cudaFree(w->J64); cudaFree(w->J32);
+  delete w;
+  p->work = nullptr;
+}
+
+static int ensure_work(mrg_problem* p, bool need64, bool need32) {
+  if (!p->work) {
+    p->work = new SolverWork();
+    p->work->n = p->ndof;
+    p->work->nnz = p->nnz;
+  }
+  SolverWork* w = p->work;
+  const int64_t n = p->ndof;
+  const size_t nparts = 3 * (size_t)nblk(n, ST) + 64;
+  if (!w->parts) MRG_CUDA(cudaMalloc(&w->parts, nparts * sizeof(double)));
+  if (!w->s) {
+    MRG_CUDA(cudaMalloc(&w->s, sizeof(PcgScal)));
+    MRG_CUDA(cudaMemset(w->s, 0, sizeof(PcgScal)));
+    MRG_CUDA(cudaMallocHost(&w->h_s, sizeof(PcgScal)));
+  }
+  if (need64 && !w->r) {
+    MRG_CUDA(cudaMalloc(&w->r, n * sizeof(double)));
+    MRG_CUDA(cudaMalloc(&w->z, n * sizeof(double)));
+    MRG_CUDA(cudaMalloc(&w->p, n * sizeof(double)));
+    MRG_CUDA(cudaMalloc(&w->q, n * sizeof(double)));
+    MRG_CUDA(cudaMalloc(&w->minv, n * sizeof(double)));
+  }
+  if (need32 && !w->r32) {
+    MRG_CUDA(cudaMalloc(&w->x32, n * sizeof(float)));
+    MRG_CUDA(cudaMalloc(&w->r32, n * sizeof(float)));
+    MRG_CUDA(cudaMalloc(&w->z32, n * sizeof(float)));
+    MRG_CUDA(cudaMalloc(&w->p32, n * sizeof(float)));
+    MRG_CUDA(cudaMalloc(&w->q32, n * sizeof(float)));
+    MRG_CUDA(cudaMalloc(&w->minv32, n * sizeof(float)));
+  }
+  return MRG_OK;
+}
+
+template <int P>
+static void enqueue_chunk64(const mrg_problem* p, const PcgVec64& V, cudaStream_t s) {
+  const unsigned nb = nblk(p->ndof, ST);
+  for (int it = 0; it < CHUNK; ++it) {
+    k_pcg64_spmv<P><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+    k_pcg64_update<<<nb, ST, 0, s>>>(p->ndof, V);
+    k_pcg64_dir<<<nb, ST, 0, s>>>(p->ndof, V);
+  }
+}
+template <int P>
+static void enqueue_chunk32(const mrg_problem* p, const PcgVec32& V, cudaStream_t s) {
+  const unsigned nb = nblk(p->ndof, ST);
+  for (int it = 0; it < CHUNK; ++it) {
+    k_pcg32_spmv<P><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+    k_pcg32_update<<<nb, ST, 0, s>>>(p->ndof, V);
+    k_pcg32_dir<<<nb, ST, 0, s>>>(p->ndof, V);
+  }
+}
+
+// Capture one chunk of iterations as a graph (re-captured when the buffers or stream change).
+static int chunk_graph(cudaGraphExec_t* exec, const void** key, cudaStream_t* kstream, const void* a, const void* b,
+                       const void* c, cudaStream_t s, void (*enqueue)(const mrg_problem*, const void*, cudaStream_t),
+                       const mrg_problem* p, const void* V) {
+  if (*exec && key[0] == a && key[1] == b && key[2] == c && *kstream == s) return MRG_OK;
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+  }
+  cudaStream_t cs = s;
+  bool own = false;
+  if (s == nullptr) {  // the legacy default stream cannot be captured: capture on a private stream
+    MRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    own = true;
+  }
+  cudaGraph_t graph;
+  MRG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  enqueue(p, V, cs);
+  cudaError_t e = cudaStreamEndCapture(cs, &graph);
+  if (own) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) return mrg_cuda_check(e, "capture PCG chunk");
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return mrg_cuda_check(e, "instantiate PCG chunk");
+  key[0] = a; key[1] = b; key[2] = c;
+  *kstream = s;
+  return MRG_OK;
+}
+
+static void enq64_p1(const mrg_problem* p, const void* V, cudaStream_t s) { enqueue_chunk64<1>(p, *(const PcgVec64*)V, s); }
+static void enq64_p2(const mrg_problem* p, const void* V, cudaStream_t s) { enqueue_chunk64<2>(p, *(const PcgVec64*)V, s); }
+static void enq32_p1(const mrg_problem* p, const void* V, cudaStream_t s) { enqueue_chunk32<1>(p, *(const PcgVec32*)V, s); }
+static void enq32_p2(const mrg_problem* p, const void* V, cudaStream_t s) { enqueue_chunk32<2>(p, *(const PcgVec32*)V, s); }
+
+// Runs the chunk graph until the device done flag is set.  Reads the scalars back (one sync per chunk).
+static int run_chunks(mrg_problem* p, cudaGraphExec_t exec, cudaStream_t s, int maxiter) {
+  SolverWork* w = p->work;
+  const int max_chunks = maxiter / CHUNK + 2;
+  for (int c = 0; c < max_chunks; ++c) {
+    MRG_CUDA(cudaGraphLaunch(exec, s));
+    MRG_CUDA(cudaMemcpyAsync(w->h_s, w->s, sizeof(PcgScal), cudaMemcpyDeviceToHost, s));
+    MRG_CUDA(cudaStreamSynchronize(s));
+    if (w->h_s->done) return MRG_OK;
+  }
+  return MRG_OK;
+}
+
+static int pcg64(mrg_problem* p, const double* J, const double* b, double* x, double rtol, int maxiter,
+                 mrg_solve_stats* st, cudaStream_t s) {
+  int rc = ensure_work(p, true, false);
+  if (rc) return rc;
+  SolverWork* w = p->work;
+  PcgVec64 V{x, w->r, w->z, w->p, w->q, w->minv, w->parts, b, J, w->s};
+  PcgScal init{};
+  init.tol = rtol;
+  init.maxiter = maxiter;
+  MRG_CUDA(cudaMemcpyAsync(w->s, &init, sizeof(PcgScal), cudaMemcpyHostToDevice, s));
+  const unsigned nb = nblk(p->ndof, ST);
+  if (p->g.p == 1) k_pcg64_init<1><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+  else k_pcg64_init<2><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+  MRG_CUDA(cudaGetLastError());
+  rc = chunk_graph(&w->g64, w->g64_key, &w->g64_stream, J, b, x, s, p->g.p == 1 ? enq64_p1 : enq64_p2, p, &V);
+  if (rc) return rc;
+  rc = run_chunks(p, w->g64, s, maxiter);
+  if (rc) return rc;
+  PcgScal* h = w->h_s;
+  if (st) {
+    st->iterations = h->iter;
+    st->outer_iterations = 0;
+    st->rel_residual = (h->r0 > 0) ? h->rnorm / h->r0 : 0.0;
+    st->abs_residual = h->rnorm;
+    st->status = h->status;
+  }
+  if (h->status != MRG_OK) return mrg_fail(h->status, "PCG: non-positive or non-finite curvature (matrix not SPD?)");
+  if (h->r0 > 0 && h->rnorm / h->r0 > rtol) {
+    if (st) st->status = MRG_ENOCONV;
+    return mrg_fail(MRG_ENOCONV, "PCG: maximum iterations reached before the tolerance");
+  }
+  return MRG_OK;
+}
+
+// FP32 PCG on J32 dx = b (x0 = 0); result in w->x32
+static int pcg32(mrg_problem* p, const float* J, const double* b, double rtol, int maxiter, mrg_solve_stats* st,
+                 cudaStream_t s) {
+  int rc = ensure_work(p, false, true);
+  if (rc) return rc;
+  SolverWork* w = p->work;
+  PcgVec32 V{w->x32, w->r32, w->z32, w->p32, w->q32, w->minv32, w->parts, b, J, w->s};
+  PcgScal init{};
+  init.tol = rtol;
+  init.maxiter = maxiter;
+  MRG_CUDA(cudaMemcpyAsync(w->s, &init, sizeof(PcgScal), cudaMemcpyHostToDevice, s));
+  const unsigned nb = nblk(p->ndof, ST);
+  if (p->g.p == 1) k_pcg32_init<1><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+  else k_pcg32_init<2><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+  MRG_CUDA(cudaGetLastError());
+  rc = chunk_graph(&w->g32, w->g32_key, &w->g32_stream, J, b, w->x32, s, p->g.p == 1 ? enq32_p1 : enq32_p2, p, &V);
+  if (rc) return rc;
+  rc = run_chunks(p, w->g32, s, maxiter);
+  if (rc) return rc;
+  PcgScal* h = w->h_s;
+  if (st) {
+    st->iterations = h->iter;
+    st->rel_residual = (h->r0 > 0) ? h->rnorm / h->r0 : 0.0;
+    st->abs_residual = h->rnorm;
+    st->status = h->status;
+  }
+  if (h->status != MRG_OK) return mrg_fail(h->status, "PCG (FP32): non-positive or non-finite curvature");
+  return MRG_OK;
+}
+
+extern "C" int mrg_spmv(const mrg_problem* p, const void* J, int32_t fp32, const double* x, double* y,
+                        mrg_stream_t stream) {
+  if (!p || !J || !x || !y) return mrg_fail(MRG_EINVAL, "mrg_spmv: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned nb = nblk(p->ndof, ST);
+  if (p->g.p == 1) {
+    if (fp32) k_spmv<1, float><<<nb, ST, 0, s>>>(p->g, p->ndof, (const float*)J, x, y);
+    else k_spmv<1, double><<<nb, ST, 0, s>>>(p->g, p->ndof, (const double*)J, x, y);
+  } else {
+    if (fp32) k_spmv<2, float><<<nb, ST, 0, s>>>(p->g, p->ndof, (const float*)J, x, y);
+    else k_spmv<2, double><<<nb, ST, 0, s>>>(p->g, p->ndof, (const double*)J, x, y);
+  }
+  MRG_CUDA(cudaGetLastError());
+  return MRG_OK;
+}
+
+extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const double* b, double* x, double rtol,
+                             int32_t maxiter, mrg_solve_stats* st, mrg_stream_t stream) {
+  if (!p || !J || !b || !x) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg: null argument");
+  if (!(rtol >= 0.0) || maxiter < 0) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg: bad tolerance or iteration limit");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!fp32) return pcg64(p, (const double*)J, b, x, rtol, maxiter, st, s);
+  // FP32 matrix: solve J dx = b - J x0 in FP32, then x = x0 + dx
+  int rc = ensure_work(p, true, true);
+  if (rc) return rc;
+  SolverWork* w = p->work;
+  double* res = w->r;  // b - J x0
+  rc = mrg_spmv(p, J, 1, x, res, stream);
+  if (rc) return rc;
+  const unsigned nb = nblk(p->ndof, 256);
+  // z = b - J x0
+  MRG_CUDA(cudaMemcpyAsync(w->z, b, p->ndof * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  k_axpy<<<nb, 256, 0, s>>>(p->ndof, -1.0, res, w->z);
+  MRG_CUDA(cudaGetLastError());
+  rc = pcg32(p, (const float*)J, w->z, rtol, maxiter, st, s);
+  if (rc) return rc;
+  k_add_f32<<<nb, 256, 0, s>>>(p->ndof, w->x32, x);
+  MRG_CUDA(cudaGetLastError());
+  MRG_CUDA(cudaStreamSynchronize(s));
+  return MRG_OK;
+}
+
+static int norm_inf(mrg_problem* p, const double* v, double* out, cudaStream_t s) {
+  SolverWork* w = p->work;
+  k_norminf<<<nblk(p->ndof, ST), ST, 0, s>>>(p->ndof, v, w->parts, w->s);
+  MRG_CUDA(cudaGetLastError());
+  MRG_CUDA(cudaMemcpyAsync(w->h_s, w->s, sizeof(PcgScal), cudaMemcpyDeviceToHost, s));
+  MRG_CUDA(cudaStreamSynchronize(s));
+  *out = w->h_s->rnorm;
+  return MRG_OK;
+}
+
+extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, mrg_solve_stats* st,
+                          mrg_stream_t stream) {
+  if (!p || !u || !o) return mrg_fail(MRG_EINVAL, "mrg_newton: null argument");
+  if (o->max_iters < 1 || !(o->nl_tol > 0.0)) return mrg_fail(MRG_EINVAL, "mrg_newton: bad options");
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool mixed = o->mixed != 0;
+  int rc = ensure_work(p, true, mixed);
+  if (rc) return rc;
+  SolverWork* w = p->work;
+  if (!w->F) {
+    MRG_CUDA(cudaMalloc(&w->F, p->ndof * sizeof(double)));
+    MRG_CUDA(cudaMalloc(&w->du, p->ndof * sizeof(double)));
+  }
+  if (mixed && !w->J32) MRG_CUDA(cudaMalloc(&w->J32, p->nnz * sizeof(float)));
+  if (!mixed && !w->J64) MRG_CUDA(cudaMalloc(&w->J64, p->nnz * sizeof(double)));
+  void* J = mixed ? (void*)w->J32 : (void*)w->J64;
+  const uint32_t jflags = MRG_ASM_JAC | MRG_ASM_OVERWRITE | (mixed ? MRG_ASM_J_FP32 : 0u);
+  rc = mrg_set_dirichlet(p, u, stream);
+  if (rc) return rc;
+  double first = 0.0, scaled = 1.0, nrm = 0.0, alpha = 1.0;
+  int it = 0, cgtot = 0;
+  bool proceed = true, have_J = false, have_du = false;
+  int status = MRG_OK;
+  while (proceed) {
+    // residual (assembleRes, FP64), inf norm (solverManager_solvers.hpp:380-390)
+    rc = mrg_assemble(p, u, w->F, nullptr, MRG_ASM_RES | MRG_ASM_OVERWRITE, stream);
+    if (rc) return rc;
+    rc = norm_inf(p, w->F, &nrm, s);
+    if (rc) return rc;
+    if (!std::isfinite(nrm)) { status = MRG_ENUMERIC; break; }
+    bool solve = true;
+    if (it == 0) { first = nrm; scaled = 1.0; } else scaled = (first > 0.0) ? nrm / first : 0.0;
+    if (it > 0 && scaled > 1.1 && have_du) {
+      // backtracking (solverManager_solvers.hpp:416-429): u -= alpha*du, alpha halves
+      alpha *= 0.5;
+      k_axpy<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, -alpha, w->du, u);
+      MRG_CUDA(cudaGetLastError());
+      solve = false;
+    } else if (scaled < o->nl_tol || nrm < 1.0e-100) {
+      solve = false;
+      proceed = false;
+    }
+    if (solve) {
+      if (!have_J || !o->reuse_jacobian) {
+        rc = mrg_assemble(p, u, nullptr, J, jflags, stream);
+        if (rc) return rc;
+        have_J = true;
+      }
+      mrg_solve_stats ls{};
+      if (!mixed) {
+        MRG_CUDA(cudaMemsetAsync(w->du, 0, p->ndof * sizeof(double), s));
+        rc = pcg64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s);
+        if (rc && rc != MRG_ENOCONV) return rc;
+      } else {
+        rc = pcg32(p, w->J32, w->F, o->lin_tol, o->lin_maxiter, &ls, s);
+        if (rc) return rc;
+        k_f32_to_f64<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, w->x32, w->du);
+        MRG_CUDA(cudaGetLastError());
+      }
+      cgtot += ls.iterations;
+      alpha = 1.0;
+      k_axpy<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, 1.0, w->du, u);
+      MRG_CUDA(cudaGetLastError());
+      have_du = true;
+    }
+    it++;
+    if (it >= o->max_iters) proceed = false;
+  }
+  MRG_CUDA(cudaStreamSynchronize(s));
+  if (st) {
+    st->iterations = cgtot;
+    st->outer_iterations = it;
+    st->rel_residual = scaled;
+    st->abs_residual = nrm;
+    st->status = status;
+  }
+  if (status != MRG_OK) return mrg_fail(status, "Newton: non-finite residual");
+  if (!(scaled < o->nl_tol) && nrm >= 1.0e-100) {
+    if (st) st->status = MRG_ENOCONV;
+    return mrg_fail(MRG_ENOCONV, "Newton: not converged within max_iters");
+  }
+  return MRG_OK;
+}
