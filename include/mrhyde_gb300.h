@@ -174,6 +174,19 @@ typedef struct mrg_newton_opts {
 int mrg_newton(mrg_problem* p, double* u_dev, const mrg_newton_opts* opts, mrg_solve_stats* stats,
                mrg_stream_t stream);
 
+/* Jacobi PCG like mrg_solve_pcg (FP64 Jacobian only) that allocates nothing: no cudaMalloc, cudaFree,
+   pinned-host or other allocating call.  No counterpart in the reference; it exists for callers that
+   cannot allocate device memory themselves -- a runtime that owns all device memory and admits work
+   against a fixed HBM budget, a framework whose pool allocator must be the only one, a latency-critical
+   loop.  Its work vectors live in one fixed, file-scope device array of the library, sized for at most
+   MRG_NOALLOC_MAX_DOFS unknowns (about 10.5 MB, held by every GPU that loads the library until the
+   process exits); larger problems return MRG_EINVAL.  All calls share that array: calls whose GPU work
+   overlaps race and must be serialised by the caller.  The first call on a device looks up the array's
+   address with that device current; make it before any stream capture on that device. */
+#define MRG_NOALLOC_MAX_DOFS (1 << 18)
+int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J_vals_dev, const double* b_dev, double* x_dev,
+                          double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
+
 /* ---- diagnostics ----------------------------------------------------------------------------- */
 int mrg_last_error(char* buf, size_t len);   /* copies the calling thread's last error message */
 const char* mrg_version(void);

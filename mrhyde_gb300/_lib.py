@@ -30,6 +30,7 @@ MRG_ASM_FORCE_CELL = 256
 MRG_ASM_ATOMIC = 512
 MRG_ASM_ADJOINT = 1024
 MRG_ASM_SENS = 2048
+MRG_NOALLOC_MAX_DOFS = 1 << 18
 
 
 class MeshDesc(C.Structure):
@@ -77,6 +78,7 @@ SIGNATURES = {
     "mrg_spmv": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "mrg_solve_pcg": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_newton": (C.c_int, [_VP, _VP, C.POINTER(NewtonOpts), C.POINTER(SolveStats), _VP]),
+    "mrg_solve_pcg_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "mrg_version": (C.c_char_p, []),
 }

@@ -19,6 +19,7 @@
 // iteration), dot products are accumulated in FP64 per block; the Newton residual, the update of u
 // and the stopping test stay FP64, so Newton / iterative refinement recovers the FP64 solution.
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "mrg_internal.h"
@@ -767,6 +768,111 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
   if (!(scaled < o->nl_tol) && nrm >= 1.0e-100) {
     if (st) st->status = MRG_ENOCONV;
     return mrg_fail(MRG_ENOCONV, "Newton: not converged within max_iters");
+  }
+  return MRG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// PCG that allocates nothing (mrg_solve_pcg_noalloc).
+//
+// Some callers cannot call cudaMalloc: a runtime that owns all device memory and admits work
+// against a fixed HBM budget, a host framework whose pool allocator must be the only one, or a
+// latency-critical loop where an allocation (and the implicit synchronisation cudaMalloc/cudaFree
+// may bring) is not acceptable.  This entry point runs the same Jacobi PCG iteration as
+// mrg_solve_pcg on an FP64 Jacobian, but keeps every work vector, the per-block partial sums and the
+// device scalars in one file-scope __device__ array of fixed size instead of library-allocated
+// workspace, and reads the scalars back into a host stack variable instead of pinned memory.
+//
+// Limits and sharing rules:
+//   * at most MRG_NOALLOC_MAX_DOFS unknowns; larger problems are rejected with MRG_EINVAL;
+//   * the array (about 10.5 MB) is part of the module image: every GPU that loads the library
+//     holds it until the process exits;
+//   * all calls share the one array and it keeps the last call's contents; the scalars (including
+//     the reduction counter) are re-initialised by every call, the vectors are fully rewritten;
+//   * calls whose GPU work overlaps (different streams, or different host threads) race on the
+//     array: serialise them;
+//   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
+//     that device current; make that first call before any stream capture on the device.
+// ------------------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+constexpr int64_t NA_N = MRG_NOALLOC_MAX_DOFS;
+constexpr int64_t NA_PARTS = 3 * ((NA_N + ST - 1) / ST) + 64;
+struct NoAllocScratch {
+  double vec[5][NA_N];  // r, z, p, q, 1/diag
+  double parts[NA_PARTS];
+  PcgScal scal;
+};
+
+__global__ void k_na_init_scal(PcgScal* s, double tol, int maxiter) {
+  PcgScal z{};
+  z.tol = tol;
+  z.maxiter = maxiter;
+  *s = z;  // also clears the last-block counter left by the previous call
+}
+}  // namespace
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+static std::mutex g_na_mutex;
+static NoAllocScratch* g_na_addr[256] = {nullptr};
+
+static int noalloc_scratch(NoAllocScratch** out) {
+  int dev = 0;
+  MRG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg_noalloc: device ordinal out of range");
+  std::lock_guard<std::mutex> lk(g_na_mutex);
+  if (!g_na_addr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return mrg_cuda_check(e, "cudaGetSymbolAddress(no-alloc PCG scratch)");
+    g_na_addr[dev] = static_cast<NoAllocScratch*>(ptr);
+  }
+  *out = g_na_addr[dev];
+  return MRG_OK;
+}
+
+extern "C" int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J, const double* b, double* x, double rtol,
+                                     int32_t maxiter, mrg_solve_stats* st, mrg_stream_t stream) {
+  if (!p || !J || !b || !x) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg_noalloc: null argument");
+  if (!(rtol >= 0.0) || maxiter < 0)
+    return mrg_fail(MRG_EINVAL, "mrg_solve_pcg_noalloc: bad tolerance or iteration limit");
+  if (p->ndof > NA_N)
+    return mrg_fail(MRG_EINVAL, "mrg_solve_pcg_noalloc: problem has " + std::to_string(p->ndof) +
+                                    " DOFs, above the fixed scratch limit MRG_NOALLOC_MAX_DOFS = " +
+                                    std::to_string((long long)NA_N));
+  NoAllocScratch* S = nullptr;
+  int rc = noalloc_scratch(&S);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  PcgVec64 V{x, S->vec[0], S->vec[1], S->vec[2], S->vec[3], S->vec[4], S->parts, b, J, &S->scal};
+  k_na_init_scal<<<1, 1, 0, s>>>(&S->scal, rtol, maxiter);
+  const unsigned nb = nblk(p->ndof, ST);
+  if (p->g.p == 1) k_pcg64_init<1><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+  else k_pcg64_init<2><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+  MRG_CUDA(cudaGetLastError());
+  PcgScal h{};
+  const int max_chunks = maxiter / CHUNK + 2;
+  for (int c = 0; c < max_chunks; ++c) {
+    if (p->g.p == 1) enqueue_chunk64<1>(p, V, s);
+    else enqueue_chunk64<2>(p, V, s);
+    MRG_CUDA(cudaGetLastError());
+    MRG_CUDA(cudaMemcpyAsync(&h, &S->scal, sizeof(PcgScal), cudaMemcpyDeviceToHost, s));
+    MRG_CUDA(cudaStreamSynchronize(s));
+    if (h.done) break;
+  }
+  if (st) {
+    st->iterations = h.iter;
+    st->outer_iterations = 0;
+    st->rel_residual = (h.r0 > 0) ? h.rnorm / h.r0 : 0.0;
+    st->abs_residual = h.rnorm;
+    st->status = h.status;
+  }
+  if (h.status != MRG_OK) return mrg_fail(h.status, "PCG (no-alloc): non-positive or non-finite curvature");
+  if (h.r0 > 0 && h.rnorm / h.r0 > rtol) {
+    if (st) st->status = MRG_ENOCONV;
+    return mrg_fail(MRG_ENOCONV, "PCG (no-alloc): maximum iterations reached before the tolerance");
   }
   return MRG_OK;
 }
