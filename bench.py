@@ -344,6 +344,36 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(out), flush=True)
 
 
+def run_profile(args, local_rank):
+    """Runs one kernel family only (W untimed + K launches) on C2, for ncu captures of that kernel."""
+    import torch
+
+    import mrhyde_gb300
+    from mrhyde_gb300 import AssemblyManager, Problem, SolverManager
+    from mrhyde_gb300.workloads import c2
+
+    torch.cuda.set_device(local_rank)
+    mrhyde_gb300.load()
+    P = Problem(**c2(seed=2, n=args.n))
+    A, S = AssemblyManager(P), SolverManager(P)
+    u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, P.info.n_dofs), device="cuda")
+    r = P.new_vector()
+    fp32 = args.profile in ("mixed", "pcg32")
+    J = P.new_matrix_values(fp32=fp32)
+    if args.profile in ("fp64", "mixed", "residual"):
+        step = {"fp64": lambda: A.assembleJacRes(u, r, J, overwrite=True),
+                "mixed": lambda: A.assembleJacRes(u, r, J, fp32_jacobian=True, overwrite=True),
+                "residual": lambda: A.assembleRes(u, r, overwrite=True)}[args.profile]
+        for _ in range(args.warmup + args.steps):
+            step()
+    else:  # pcg64 / pcg32: K iterations of the PCG on the C2 Jacobian
+        A.assembleJacRes(u, r, J, fp32_jacobian=fp32, overwrite=True)
+        x = P.new_vector()
+        S.PCG(J, r, x, tol=0.0, maxiter=args.steps, raise_on_noconv=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "n": args.n, "steps": args.steps, "ok": True}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -353,12 +383,17 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32"],
+                    help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.profile:
+        run_profile(args, local_rank)
         return
     if world > 1:
         import torch

@@ -123,6 +123,12 @@ enum {
 
 /* ---- problem lifetime ------------------------------------------------------------------------- */
 int mrg_problem_create(const mrg_mesh_desc* mesh, const mrg_physics_desc* phys, mrg_problem** out);
+/* Same as mrg_problem_create with the handle's device memory allocated (stream-ordered) and uploaded
+   on `stream`; nothing synchronises other streams, so problems can be created while other solves run
+   (the serving loop).  mrg_problem_create is this call on the legacy default stream. */
+int mrg_problem_create_on_stream(const mrg_mesh_desc* mesh, const mrg_physics_desc* phys, mrg_stream_t stream,
+                                 mrg_problem** out);
+/* Waits for the last stream the handle's work was enqueued on, then frees its memory in stream order. */
 int mrg_problem_destroy(mrg_problem* p);
 int mrg_problem_get_info(const mrg_problem* p, mrg_problem_info* info);
 
@@ -173,6 +179,49 @@ typedef struct mrg_newton_opts {
    Uses library-owned device workspace (allocated on first use, freed with the problem). */
 int mrg_newton(mrg_problem* p, double* u_dev, const mrg_newton_opts* opts, mrg_solve_stats* stats,
                mrg_stream_t stream);
+
+/* ---- batched multiscale-subgrid solves -------------------------------------------------------
+   Replaces the per-macro-element loop of local solves (MultiscaleManager::evaluateMacroMicroMacroMap,
+   src/managers/multiscale/multiscaleManager.cpp:866 -> SubGridDtN::subgridSolver, src/subgrid/subgridDtN.cpp:985
+   -> SubGridDtN_Solver::solve, src/subgrid/subgridDtN_solver.cpp:136, assembly :681, Newton :903) for
+   independent steady-thermal Q1 hexahedral local problems on the unit cube: Dirichlet data on every
+   boundary node, kappa per cell, constant source.  One persistent launch (captured as a CUDA graph)
+   assembles every problem's FP32 Jacobian and solves it by FP32 Jacobi-PCG with FP64 refinement. */
+typedef struct mrg_batch mrg_batch;
+typedef struct mrg_batch_desc {
+  int32_t n_problems;
+  const int32_t* sizes;     /* host [n_problems][3] cells per axis, each in [2, 16]          */
+  const double* kappa;      /* host, concatenated per-cell kappa of all problems (cell order)  */
+  const double* dirichlet;  /* host, concatenated per-node values; read at boundary nodes      */
+  double source;            /* constant f                                                      */
+} mrg_batch_desc;
+typedef struct mrg_batch_info {
+  int32_t n_problems;
+  int32_t threads, ctas_per_sm; /* launch configuration (autotuned or set) */
+  int32_t reserved;
+  int64_t n_cells, n_nodes, nnz;
+} mrg_batch_info;
+typedef struct mrg_batch_opts {
+  double tol;        /* ||r||_inf / ||r0||_inf per problem (FP64 residual) */
+  double inner_tol;  /* FP32 PCG relative 2-norm tolerance                  */
+  int32_t max_outer, max_inner;
+} mrg_batch_opts;
+typedef struct mrg_batch_stat {
+  int32_t outer_iterations, inner_iterations;
+  double rel_residual;
+  int32_t status, reserved;
+} mrg_batch_stat;
+int mrg_batch_create(const mrg_batch_desc* desc, mrg_batch** out);
+int mrg_batch_destroy(mrg_batch* b);
+/* node_off / nnz_off: optional host [n_problems] offsets of each problem in u and J */
+int mrg_batch_get_info(const mrg_batch* b, mrg_batch_info* info, int64_t* node_off, int64_t* nnz_off);
+/* u_dev: double[n_nodes] (output: solutions); J_dev: float[nnz] (output: each problem's FP32 Jacobian on
+   its canonical local graph).  stats: optional host [n_problems]; when given the call synchronises. */
+int mrg_batch_solve(mrg_batch* b, double* u_dev, float* J_dev, const mrg_batch_opts* opts, mrg_batch_stat* stats,
+                    mrg_stream_t stream);
+/* Times the batch under each launch configuration and keeps the fastest (u_dev/J_dev used as scratch). */
+int mrg_batch_autotune(mrg_batch* b, double* u_dev, float* J_dev, const mrg_batch_opts* opts, mrg_stream_t stream);
+int mrg_batch_set_config(mrg_batch* b, int32_t threads, int32_t ctas_per_sm);
 
 /* Jacobi PCG like mrg_solve_pcg (FP64 Jacobian only) that allocates nothing: no cudaMalloc, cudaFree,
    pinned-host or other allocating call.  No counterpart in the reference; it exists for callers that

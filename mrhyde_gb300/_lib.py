@@ -63,10 +63,30 @@ class NewtonOpts(C.Structure):
                 ("lin_tol", C.c_double), ("lin_maxiter", C.c_int32), ("reuse_jacobian", C.c_int32)]
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [("n_problems", C.c_int32), ("sizes", C.POINTER(C.c_int32)), ("kappa", C.POINTER(C.c_double)),
+                ("dirichlet", C.POINTER(C.c_double)), ("source", C.c_double)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n_problems", C.c_int32), ("threads", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("reserved", C.c_int32), ("n_cells", C.c_int64), ("n_nodes", C.c_int64), ("nnz", C.c_int64)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("inner_tol", C.c_double), ("max_outer", C.c_int32), ("max_inner", C.c_int32)]
+
+
+class BatchStat(C.Structure):
+    _fields_ = [("outer_iterations", C.c_int32), ("inner_iterations", C.c_int32), ("rel_residual", C.c_double),
+                ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
 # name -> (restype, argtypes) for every entry point of include/mrhyde_gb300.h
 _VP = C.c_void_p
 SIGNATURES = {
     "mrg_problem_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysicsDesc), C.POINTER(_VP)]),
+    "mrg_problem_create_on_stream": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysicsDesc), _VP, C.POINTER(_VP)]),
     "mrg_problem_destroy": (C.c_int, [_VP]),
     "mrg_problem_get_info": (C.c_int, [_VP, C.POINTER(ProblemInfo)]),
     "mrg_get_graph": (C.c_int, [_VP, _VP, _VP, _VP]),
@@ -79,6 +99,12 @@ SIGNATURES = {
     "mrg_solve_pcg": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_newton": (C.c_int, [_VP, _VP, C.POINTER(NewtonOpts), C.POINTER(SolveStats), _VP]),
     "mrg_solve_pcg_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
+    "mrg_batch_create": (C.c_int, [C.POINTER(BatchDesc), C.POINTER(_VP)]),
+    "mrg_batch_destroy": (C.c_int, [_VP]),
+    "mrg_batch_get_info": (C.c_int, [_VP, C.POINTER(BatchInfo), _VP, _VP]),
+    "mrg_batch_solve": (C.c_int, [_VP, _VP, _VP, C.POINTER(BatchOpts), _VP, _VP]),
+    "mrg_batch_autotune": (C.c_int, [_VP, _VP, _VP, C.POINTER(BatchOpts), _VP]),
+    "mrg_batch_set_config": (C.c_int, [_VP, C.c_int32, C.c_int32]),
     "mrg_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "mrg_version": (C.c_char_p, []),
 }

@@ -62,7 +62,7 @@ class Problem:
 
     def __init__(self, dim=3, order=1, n=(8, 8, 8), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), kind="thermal",
                  source=("const", 1.0, 0.0), kappa=1.0, dirichlet_faces=L.MRG_FACE_ALL, dirichlet=("const", 0.0),
-                 quad_order=0, vertex_coords=None):
+                 quad_order=0, vertex_coords=None, stream=None):
         lib = L.lib()
         m = L.MeshDesc()
         m.dim, m.order = dim, order
@@ -100,7 +100,11 @@ class Problem:
             raise ValueError(f"unknown Dirichlet form {dirichlet[0]!r}")
         ph.quad_order = int(quad_order)
         h = C.c_void_p()
-        L.check(lib.mrg_problem_create(C.byref(m), C.byref(ph), C.byref(h)), "mrg_problem_create")
+        if stream is None:
+            L.check(lib.mrg_problem_create(C.byref(m), C.byref(ph), C.byref(h)), "mrg_problem_create")
+        else:
+            L.check(lib.mrg_problem_create_on_stream(C.byref(m), C.byref(ph), stream.cuda_stream, C.byref(h)),
+                    "mrg_problem_create_on_stream")
         self._h = h
         self.dim, self.order = dim, order
         self.n = tuple(int(v) for v in n[:dim])

@@ -32,10 +32,23 @@ namespace {
 constexpr int FT = 128;  // rows per CTA in the factored path
 
 __device__ __forceinline__ void decompose(const Grid& g, int64_t n, int& ix, int& iy, int& iz) {
-  ix = (int)(n % g.nn[0]);
-  int64_t t = n / g.nn[0];
-  iy = (int)(t % g.nn[1]);
-  iz = (int)(t / g.nn[1]);
+  // 32-bit arithmetic: n_dofs <= INT32_MAX is enforced by mrg_problem_create
+  const unsigned un = (unsigned)n, nx = (unsigned)g.nn[0], ny = (unsigned)g.nn[1];
+  const unsigned t = un / nx;
+  ix = (int)(un - t * nx);
+  iy = (int)(t % ny);
+  iz = (int)(t / ny);
+}
+
+// Compensated (Neumaier) FP32 accumulation, used to give the FP32 Jacobian rows an exactly consistent
+// diagonal: the stiffness rows sum to zero, so the diagonal is set to minus the accurately summed
+// rounded off-diagonals; the FP32 operator is then itself a stiffness matrix with slightly perturbed
+// conductances, instead of one whose row sums carry independent rounding noise (which the Newton /
+// refinement loop would see as a spurious reaction term).
+__device__ __forceinline__ void neumaier_add(float& sum, float& comp, float v) {
+  const float t = sum + v;
+  comp += (fabsf(sum) >= fabsf(v)) ? (sum - t) + v : (v - t) + sum;
+  sum = t;
 }
 
 __device__ __forceinline__ int64_t row_ptr_of(const Grid& g, int64_t n, int64_t nrows) {
@@ -224,6 +237,8 @@ __global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double*
       double t[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) t[c] = 0.0;
+      float osum = 0.0f, ocomp = 0.0f;
+      int dpos = 0;
       int pos = 0;
       const int64_t plane = (int64_t)NX * NY;
 #pragma unroll
@@ -240,11 +255,20 @@ __global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double*
                 if (DOJ) sv[loc + pos] = (JT)a;
                 if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
               } else {
-                if (DOJ) sv[loc + pos] = (JT)(A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1]);
+                if (DOJ) {
+                  if (cls == 0) {
+                    dpos = pos;
+                  } else {
+                    const float v = A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1];
+                    sv[loc + pos] = (JT)v;
+                    neumaier_add(osum, ocomp, v);
+                  }
+                }
                 if (DOR) t[cls] = fma(s, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), t[cls]);
               }
               ++pos;
             }
+      if (MIXED && DOJ) sv[loc + dpos] = (JT)(-(osum + ocomp));
       if (DOR) {
         if (MIXED) {
 #pragma unroll
@@ -341,6 +365,8 @@ __global__ void __launch_bounds__(FT) k_fact_quad(const FactArgs A, const double
       if (A.src_sin) b = A.amp * A.B[0][ix] * A.B[1][iy];
       else b = A.load * (double)((cx == 3 ? 2 : 1) * (cy == 3 ? 2 : 1));
       double acc = b, t[4] = {0.0, 0.0, 0.0, 0.0};
+      float osum = 0.0f, ocomp = 0.0f;
+      int dpos = 0;
       int pos = 0;
 #pragma unroll
       for (int dy = -1; dy <= 1; ++dy)
@@ -354,11 +380,20 @@ __global__ void __launch_bounds__(FT) k_fact_quad(const FactArgs A, const double
               if (DOJ) sv[loc + pos] = (JT)a;
               if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy), acc);
             } else {
-              if (DOJ) sv[loc + pos] = (JT)(A.Kp32[cls] * S32[dy + 1][dx + 1]);
+              if (DOJ) {
+                if (cls == 0) {
+                  dpos = pos;
+                } else {
+                  const float v = A.Kp32[cls] * S32[dy + 1][dx + 1];
+                  sv[loc + pos] = (JT)v;
+                  neumaier_add(osum, ocomp, v);
+                }
+              }
               if (DOR) t[cls] = fma(s, __ldg(u + n + dx + (int64_t)NX * dy), t[cls]);
             }
             ++pos;
           }
+      if (MIXED && DOJ) sv[loc + dpos] = (JT)(-(osum + ocomp));
       if (DOR) {
         if (MIXED) {
 #pragma unroll

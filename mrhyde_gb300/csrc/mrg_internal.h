@@ -98,6 +98,10 @@ struct mrg_problem {
   double Kp[8];                 // factored path: K(|dx|,|dy|,|dz|) of one cell, kappa = 1
   double cell_load;             // factored path: int_cell phi_l for one node (vol / 2^dim)
   std::vector<double> qtab_host;
+  std::vector<double> gx1, gw1;  // 1-D Gauss rule of the problem
+  void* q2 = nullptr;            // Q2 tensor-product data (mrg_assemble_q2.cu)
+  cudaStream_t stream = nullptr;       // creation stream: the handle's memory is allocated/freed in its order
+  cudaStream_t last_stream = nullptr;  // last stream work was enqueued on (drained before destroy)
   SolverWork* work = nullptr;
 };
 
@@ -117,5 +121,9 @@ int mrg_launch_cell(mrg_problem* p, const double* u, double* r, void* J, uint32_
 int mrg_launch_constraints(mrg_problem* p, void* J, bool fp32, cudaStream_t s);
 int mrg_launch_fix_zero_rows(mrg_problem* p, void* J, bool fp32, cudaStream_t s);
 int mrg_launch_kappa32(mrg_problem* p, cudaStream_t s);
+// Q2 hexahedra on identical affine cells (mrg_assemble_q2.cu)
+int mrg_q2_setup(mrg_problem* p);
+void mrg_q2_free(mrg_problem* p);
+int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);

@@ -160,21 +160,28 @@ static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / 
 // ------------------------------------------------------------------------------------------------
 // create / destroy
 // ------------------------------------------------------------------------------------------------
+// Frees the handle's device memory in stream order on its creation stream, after the last stream the
+// handle's work was enqueued on has drained (no device-wide synchronisation, so concurrent solves on
+// other streams keep running).
 static void free_problem(mrg_problem* p) {
   if (!p) return;
+  cudaStream_t s = p->stream;
+  if (p->last_stream != s) cudaStreamSynchronize(p->last_stream);
   mrg_solver_free(p);
-  cudaFree(p->d_prefix);
-  cudaFree(p->d_kappa);
-  cudaFree(p->d_kappa32);
-  cudaFree(p->d_fixed);
-  cudaFree(p->d_fixed_vals);
-  cudaFree(p->d_vcoord);
-  cudaFree(p->d_srcB);
-  cudaFree(p->d_qtab);
+  mrg_q2_free(p);
+  cudaFreeAsync(p->d_prefix, s);
+  cudaFreeAsync(p->d_kappa, s);
+  cudaFreeAsync(p->d_kappa32, s);
+  cudaFreeAsync(p->d_fixed, s);
+  cudaFreeAsync(p->d_fixed_vals, s);
+  cudaFreeAsync(p->d_vcoord, s);
+  cudaFreeAsync(p->d_srcB, s);
+  cudaFreeAsync(p->d_qtab, s);
+  cudaStreamSynchronize(s);
   delete p;
 }
 
-extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc* ph, mrg_problem** out) {
+static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaStream_t cs, mrg_problem** out) {
   if (!m || !ph || !out) return mrg_fail(MRG_EINVAL, "mrg_problem_create: null argument");
   *out = nullptr;
   if (m->dim != 2 && m->dim != 3) return mrg_fail(MRG_EINVAL, "dim must be 2 or 3");
@@ -195,6 +202,8 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
   if (qo > 14) return mrg_fail(MRG_EINVAL, "quadrature order above 14 not supported");
 
   mrg_problem* P = new mrg_problem();
+  P->stream = cs;
+  P->last_stream = cs;
   Grid& g = P->g;
   g.dim = m->dim;
   g.p = p;
@@ -236,9 +245,13 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
     P->hi[k] = (k < m->dim) ? m->hi[k] : 1.0;
     P->h[k] = (k < m->dim) ? (P->hi[k] - P->lo[k]) / g.nc[k] : 1.0;
   }
+  P->gx1 = gx;
+  P->gw1 = gw;
   P->affine = (m->vertex_coords == nullptr);
   if (P->affine && p == 1 && ph->kind == MRG_THERMAL && qo >= 2)
     P->path = MRG_PATH_FACTORED;
+  else if (P->affine && p == 2 && m->dim == 3 && n1 == 3 && ph->source_kind == MRG_SRC_CONST)
+    P->path = MRG_PATH_Q2_TC;
   else
     P->path = MRG_PATH_CELL;
 
@@ -249,8 +262,8 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
   };
   cudaError_t e;
   // prefix tables
-  if ((e = cudaMalloc(&P->d_prefix, pref.size() * sizeof(int64_t))) != cudaSuccess) return fail_cuda(e, "cudaMalloc prefix");
-  if ((e = cudaMemcpy(P->d_prefix, pref.data(), pref.size() * sizeof(int64_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+  if ((e = cudaMallocAsync(&P->d_prefix, pref.size() * sizeof(int64_t), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc prefix");
+  if ((e = cudaMemcpyAsync(P->d_prefix, pref.data(), pref.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
     return fail_cuda(e, "upload prefix");
   for (int k = 0; k < 3; ++k) g.P[k] = P->d_prefix + offs[k];
   // coefficients
@@ -262,9 +275,9 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
       free_problem(P);
       return mrg_fail(MRG_ENUMERIC, "kappa contains NaN or Inf");
     }
-  if ((e = cudaMalloc(&P->d_kappa, P->ncell * sizeof(double))) != cudaSuccess) return fail_cuda(e, "cudaMalloc kappa");
-  if ((e = cudaMalloc(&P->d_kappa32, P->ncell * sizeof(float))) != cudaSuccess) return fail_cuda(e, "cudaMalloc kappa32");
-  if ((e = cudaMemcpy(P->d_kappa, kap.data(), P->ncell * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+  if ((e = cudaMallocAsync(&P->d_kappa, P->ncell * sizeof(double), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc kappa");
+  if ((e = cudaMallocAsync(&P->d_kappa32, P->ncell * sizeof(float), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc kappa32");
+  if ((e = cudaMemcpyAsync(P->d_kappa, kap.data(), P->ncell * sizeof(double), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
     return fail_cuda(e, "upload kappa");
   // Dirichlet DOFs in increasing order
   std::vector<int32_t> fixed;
@@ -279,12 +292,12 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
         }
   P->nfixed = (int64_t)fixed.size();
   if (P->nfixed > 0) {
-    if ((e = cudaMalloc(&P->d_fixed, P->nfixed * sizeof(int32_t))) != cudaSuccess) return fail_cuda(e, "cudaMalloc fixed");
-    if ((e = cudaMalloc(&P->d_fixed_vals, P->nfixed * sizeof(double))) != cudaSuccess)
+    if ((e = cudaMallocAsync(&P->d_fixed, P->nfixed * sizeof(int32_t), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc fixed");
+    if ((e = cudaMallocAsync(&P->d_fixed_vals, P->nfixed * sizeof(double), cs)) != cudaSuccess)
       return fail_cuda(e, "cudaMalloc fixed vals");
-    if ((e = cudaMemcpy(P->d_fixed, fixed.data(), P->nfixed * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(P->d_fixed, fixed.data(), P->nfixed * sizeof(int32_t), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
       return fail_cuda(e, "upload fixed");
-    if ((e = cudaMemcpy(P->d_fixed_vals, fvals.data(), P->nfixed * sizeof(double), cudaMemcpyHostToDevice)) !=
+    if ((e = cudaMemcpyAsync(P->d_fixed_vals, fvals.data(), P->nfixed * sizeof(double), cudaMemcpyHostToDevice, cs)) !=
         cudaSuccess)
       return fail_cuda(e, "upload fixed vals");
   }
@@ -330,8 +343,8 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
     }
   }
   P->qtab_host = tab;
-  if ((e = cudaMalloc(&P->d_qtab, tab.size() * sizeof(double))) != cudaSuccess) return fail_cuda(e, "cudaMalloc qtab");
-  if ((e = cudaMemcpy(P->d_qtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+  if ((e = cudaMallocAsync(&P->d_qtab, tab.size() * sizeof(double), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc qtab");
+  if ((e = cudaMemcpyAsync(P->d_qtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
     return fail_cuda(e, "upload qtab");
   // factored path: K(|dx|,|dy|,|dz|) of one box cell with kappa = 1 and the load of one node
   if (P->path == MRG_PATH_FACTORED) {
@@ -379,8 +392,8 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
         }
         off += g.nn[k];
       }
-      if ((e = cudaMalloc(&P->d_srcB, B.size() * sizeof(double))) != cudaSuccess) return fail_cuda(e, "cudaMalloc srcB");
-      if ((e = cudaMemcpy(P->d_srcB, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+      if ((e = cudaMallocAsync(&P->d_srcB, B.size() * sizeof(double), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc srcB");
+      if ((e = cudaMemcpyAsync(P->d_srcB, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
         return fail_cuda(e, "upload srcB");
     }
   }
@@ -395,23 +408,32 @@ extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc
         vc[v * d + k] = m->vertex_coords ? m->vertex_coords[v * d + k]
                                          : P->lo[k] + (P->hi[k] - P->lo[k]) * iv[k] / g.nc[k];
     }
-    if ((e = cudaMalloc(&P->d_vcoord, vc.size() * sizeof(double))) != cudaSuccess) return fail_cuda(e, "cudaMalloc vcoord");
-    if ((e = cudaMemcpy(P->d_vcoord, vc.data(), vc.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+    if ((e = cudaMallocAsync(&P->d_vcoord, vc.size() * sizeof(double), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc vcoord");
+    if ((e = cudaMemcpyAsync(P->d_vcoord, vc.data(), vc.size() * sizeof(double), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
       return fail_cuda(e, "upload vcoord");
   }
-  int st = mrg_launch_kappa32(P, 0);
+  int st = mrg_launch_kappa32(P, cs);
+  if (st == MRG_OK && P->path == MRG_PATH_Q2_TC) st = mrg_q2_setup(P);
   if (st != MRG_OK) {
     free_problem(P);
     return st;
   }
-  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail_cuda(e, "problem setup");
+  if ((e = cudaStreamSynchronize(cs)) != cudaSuccess) return fail_cuda(e, "problem setup");
   *out = P;
   return MRG_OK;
 }
 
+extern "C" int mrg_problem_create(const mrg_mesh_desc* m, const mrg_physics_desc* ph, mrg_problem** out) {
+  return create_impl(m, ph, (cudaStream_t)0, out);
+}
+
+extern "C" int mrg_problem_create_on_stream(const mrg_mesh_desc* m, const mrg_physics_desc* ph, mrg_stream_t stream,
+                                            mrg_problem** out) {
+  return create_impl(m, ph, (cudaStream_t)stream, out);
+}
+
 extern "C" int mrg_problem_destroy(mrg_problem* p) {
   if (!p) return MRG_EINVAL;
-  cudaDeviceSynchronize();
   free_problem(p);
   return MRG_OK;
 }
@@ -479,10 +501,14 @@ extern "C" int mrg_assemble(mrg_problem* p, const double* u, double* r, void* J,
   if (doJ && !J) return mrg_fail(MRG_EINVAL, "mrg_assemble: Jacobian requested but J_vals is null");
   if (doR && !r) return mrg_fail(MRG_EINVAL, "mrg_assemble: residual requested but r is null");
   cudaStream_t s = (cudaStream_t)stream;
+  p->last_stream = s;
   const bool fp32 = flags & MRG_ASM_J_FP32;
   int st;
   if (p->path == MRG_PATH_FACTORED && !(flags & MRG_ASM_FORCE_CELL)) {
     st = mrg_launch_factored(p, u, r, J, flags, s);
+    if (st != MRG_OK) return st;
+  } else if (p->path == MRG_PATH_Q2_TC && !(flags & MRG_ASM_FORCE_CELL)) {
+    st = mrg_launch_q2(p, u, r, J, flags, s);
     if (st != MRG_OK) return st;
   } else {
     if (flags & MRG_ASM_OVERWRITE) {

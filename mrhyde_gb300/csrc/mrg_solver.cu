@@ -38,11 +38,36 @@ struct PcgScal {
 };
 
 __device__ __forceinline__ void decompose(const Grid& g, int64_t n, int& ix, int& iy, int& iz) {
-  ix = (int)(n % g.nn[0]);
-  int64_t t = n / g.nn[0];
-  iy = (int)(t % g.nn[1]);
-  iz = (int)(t / g.nn[1]);
+  // 32-bit arithmetic: n_dofs <= INT32_MAX is enforced by mrg_problem_create
+  const unsigned un = (unsigned)n, nx = (unsigned)g.nn[0], ny = (unsigned)g.nn[1];
+  const unsigned t = un / nx;
+  ix = (int)(un - t * nx);
+  iy = (int)(t % ny);
+  iz = (int)(t / ny);
 }
+
+// Load the CSR segment [seg0, seg1) of a CTA's contiguous rows into shared memory with 16-byte
+// streaming loads.  dst has the same address phase modulo 16 bytes as src.
+template <typename T>
+__device__ __forceinline__ void seg_load(const T* __restrict__ src, T* __restrict__ dst, int64_t len) {
+  constexpr int V = 16 / sizeof(T);
+  int head = (int)(((16 - ((uintptr_t)src & 15)) & 15) / sizeof(T));
+  if (head > len) head = (int)len;
+  for (int k = threadIdx.x; k < head; k += blockDim.x) dst[k] = __ldcs(src + k);
+  const int64_t body = (len - head) / V;
+  if constexpr (sizeof(T) == 8) {
+    const double2* s2 = reinterpret_cast<const double2*>(src + head);
+    double2* d2 = reinterpret_cast<double2*>(dst + head);
+    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) d2[v] = __ldcs(s2 + v);
+  } else {
+    const float4* s4 = reinterpret_cast<const float4*>(src + head);
+    float4* d4 = reinterpret_cast<float4*>(dst + head);
+    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) d4[v] = __ldcs(s4 + v);
+  }
+  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) dst[k] = __ldcs(src + k);
+}
+
+
 
 struct RowInfo {
   int lx, ly, lz, cx, cy, cz;
@@ -56,6 +81,38 @@ __device__ __forceinline__ RowInfo row_info(const Grid& g, int ix, int iy, int i
   if (g.dim == 3) axis_range(iz, g.nn[2], g.p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
   R.rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)R.cz * (g.P[1][iy] * g.T[0] + (int64_t)R.cy * g.P[0][ix]);
   return R;
+}
+
+__device__ __forceinline__ int64_t row_ptr_at(const Grid& g, int64_t n, int64_t nrows) {
+  if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
+  int ix, iy, iz;
+  decompose(g, n, ix, iy, iz);
+  return row_info(g, ix, iy, iz).rp;
+}
+
+// Stages the values of the CTA's rows in shared memory (P = 1: at most 27 per row, contiguous in
+// CSR) and returns the staged copy of the row starting at my_rp; for P = 2 returns the row in global
+// memory.  Every thread of the CTA must call it (it synchronises the block).
+template <int P, typename JT>
+__device__ __forceinline__ const JT* stage_rows(const Grid& g, int64_t nrows, const JT* __restrict__ J,
+                                                int64_t my_rp, unsigned char* smem_raw, int64_t tile) {
+  if constexpr (P != 1) {
+    return J + my_rp;
+  } else {
+    const int64_t n0 = tile * ST;
+    const int64_t n1 = (n0 + ST < nrows) ? n0 + ST : nrows;
+    const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
+    const int phase = (int)(((uintptr_t)(J + seg0) & 15) / sizeof(JT));
+    JT* sv = reinterpret_cast<JT*>(smem_raw) + phase;
+    seg_load<JT>(J + seg0, sv, seg1 - seg0);
+    __syncthreads();
+    return sv + (my_rp - seg0);
+  }
+}
+
+template <int P, typename JT>
+constexpr int stage_bytes() {
+  return P == 1 ? (ST * 27 + 16 / (int)sizeof(JT)) * (int)sizeof(JT) : 0;
 }
 
 // sum of v over the block, returned in thread 0 (FP64)
@@ -105,11 +162,23 @@ __device__ __forceinline__ bool last_block(double* parts, const double (&mine)[K
 
 template <int K>
 __device__ __forceinline__ void sum_parts(const double* parts, double (&out)[K], unsigned int* counter) {
-  // whole block cooperates; fixed order: thread t sums indices t, t+blockDim, ...; then tree by warp
+  // whole block cooperates; fixed order: thread t sums indices t, t+blockDim, ... with 4 independent
+  // accumulators (combined in a fixed order), then the block tree.  The partials were published by
+  // the other blocks before their fence + counter increment; ld.global.cg reads them from L2, and the
+  // loads are independent so they pipeline instead of forming a chain of L2 round trips.
   for (int k = 0; k < K; ++k) {
-    double s = 0.0;
-    for (unsigned int i = threadIdx.x; i < gridDim.x; i += blockDim.x) s += ((volatile const double*)parts)[(size_t)k * gridDim.x + i];
-    s = block_sum(s);
+    const double* pk = parts + (size_t)k * gridDim.x;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    unsigned int i = threadIdx.x;
+    const unsigned int st = blockDim.x;
+    for (; i + 3 * st < gridDim.x; i += 4 * st) {
+      s0 += __ldcg(pk + i);
+      s1 += __ldcg(pk + i + st);
+      s2 += __ldcg(pk + i + 2 * st);
+      s3 += __ldcg(pk + i + 3 * st);
+    }
+    for (; i < gridDim.x; i += st) s0 += __ldcg(pk + i);
+    double s = block_sum((s0 + s1) + (s2 + s3));
     out[k] = s;  // valid in thread 0
   }
   if (threadIdx.x == 0) *counter = 0u;
@@ -176,15 +245,22 @@ __device__ __forceinline__ float row_apply_f(const Grid& g, const RowInfo& R, co
 template <int P, typename JT>
 __global__ void __launch_bounds__(ST) k_spmv(Grid g, int64_t nrows, const JT* __restrict__ J, const double* __restrict__ x,
                                              double* __restrict__ y) {
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
-  if (n >= nrows) return;
-  int ix, iy, iz;
-  decompose(g, n, ix, iy, iz);
-  RowInfo R = row_info(g, ix, iy, iz);
-  y[n] = row_apply<P, JT, double>(g, R, J + R.rp, x);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  const bool act = n < nrows;
+  RowInfo R{};
+  if (act) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    R = row_info(g, ix, iy, iz);
+  }
+  const JT* vals = stage_rows<P, JT>(g, nrows, J, R.rp, smem_raw, blockIdx.x);
+  if (act) y[n] = row_apply<P, JT, double>(g, R, vals, x);
 }
 
 // ---- FP64 PCG kernels ---------------------------------------------------------------------------
+// All PCG kernels are grid-stride loops over a fixed grid of at most 8 CTAs per SM, so that each
+// deterministic reduction has at most a few thousand per-CTA partials and counter increments.
 struct PcgVec64 {
   double *x, *r, *z, *p, *q, *minv, *parts;
   const double* b;
@@ -195,9 +271,8 @@ struct PcgVec64 {
 // r = b - J x, minv = 1/diag, z = minv r, p = z; partial r.r, r.z
 template <int P>
 __global__ void __launch_bounds__(ST) k_pcg64_init(Grid g, int64_t nrows, PcgVec64 V) {
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
   double rr = 0.0, rz = 0.0;
-  if (n < nrows) {
+  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
     RowInfo R = row_info(g, ix, iy, iz);
@@ -210,8 +285,8 @@ __global__ void __launch_bounds__(ST) k_pcg64_init(Grid g, int64_t nrows, PcgVec
     V.r[n] = r;
     V.z[n] = z;
     V.p[n] = z;
-    rr = r * r;
-    rz = r * z;
+    rr = fma(r, r, rr);
+    rz = fma(r, z, rz);
   }
   double m[2] = {block_sum(rr), block_sum(rz)};
   if (last_block<2>(V.parts, m, &V.s->counter)) {
@@ -233,16 +308,26 @@ __global__ void __launch_bounds__(ST) k_pcg64_init(Grid g, int64_t nrows, PcgVec
 // q = J p ; pq partial ; last block: alpha = rho / pq
 template <int P>
 __global__ void __launch_bounds__(ST) k_pcg64_spmv(Grid g, int64_t nrows, PcgVec64 V) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   if (((volatile PcgScal*)V.s)->done) return;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
   double pq = 0.0;
-  if (n < nrows) {
-    int ix, iy, iz;
-    decompose(g, n, ix, iy, iz);
-    RowInfo R = row_info(g, ix, iy, iz);
-    double q = row_apply<P, double, double>(g, R, V.J + R.rp, V.p);
-    V.q[n] = q;
-    pq = V.p[n] * q;
+  const int64_t ntiles = (nrows + ST - 1) / ST;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t n = tile * ST + threadIdx.x;
+    const bool act = n < nrows;
+    RowInfo R{};
+    if (act) {
+      int ix, iy, iz;
+      decompose(g, n, ix, iy, iz);
+      R = row_info(g, ix, iy, iz);
+    }
+    const double* vals = stage_rows<P, double>(g, nrows, V.J, R.rp, smem_raw, tile);
+    if (act) {
+      double q = row_apply<P, double, double>(g, R, vals, V.p);
+      V.q[n] = q;
+      pq = fma(V.p[n], q, pq);
+    }
+    if (P == 1) __syncthreads();  // the next tile reuses the staging buffer
   }
   double m[1] = {block_sum(pq)};
   if (last_block<1>(V.parts, m, &V.s->counter)) {
@@ -260,17 +345,16 @@ __global__ void __launch_bounds__(ST) k_pcg64_spmv(Grid g, int64_t nrows, PcgVec
 // x += alpha p ; r -= alpha q ; z = minv r ; partial r.r, r.z ; last block: beta, stopping test
 __global__ void __launch_bounds__(ST) k_pcg64_update(int64_t nrows, PcgVec64 V) {
   if (((volatile PcgScal*)V.s)->done) return;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
   const double alpha = V.s->alpha;
   double rr = 0.0, rz = 0.0;
-  if (n < nrows) {
+  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
     V.x[n] = fma(alpha, V.p[n], V.x[n]);
     double r = fma(-alpha, V.q[n], V.r[n]);
     double z = r * V.minv[n];
     V.r[n] = r;
     V.z[n] = z;
-    rr = r * r;
-    rz = r * z;
+    rr = fma(r, r, rr);
+    rz = fma(r, z, rz);
   }
   double m[2] = {block_sum(rr), block_sum(rz)};
   if (last_block<2>(V.parts, m, &V.s->counter)) {
@@ -292,8 +376,9 @@ __global__ void __launch_bounds__(ST) k_pcg64_update(int64_t nrows, PcgVec64 V) 
 // p = z + beta p
 __global__ void __launch_bounds__(ST) k_pcg64_dir(int64_t nrows, PcgVec64 V) {
   if (((volatile PcgScal*)V.s)->done) return;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
-  if (n < nrows) V.p[n] = fma(V.s->beta, V.p[n], V.z[n]);
+  const double beta = V.s->beta;
+  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST)
+    V.p[n] = fma(beta, V.p[n], V.z[n]);
 }
 
 // ---- FP32 inner PCG kernels (mixed path) ---------------------------------------------------------
@@ -307,9 +392,8 @@ struct PcgVec32 {
 
 template <int P>
 __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec32 V) {
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
   double rr = 0.0, rz = 0.0;
-  if (n < nrows) {
+  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
     RowInfo R = row_info(g, ix, iy, iz);
@@ -322,8 +406,8 @@ __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec
     V.r[n] = r;
     V.z[n] = z;
     V.p[n] = z;
-    rr = (double)(r * r);
-    rz = (double)(r * z);
+    rr += (double)(r * r);
+    rz += (double)(r * z);
   }
   double m[2] = {block_sum(rr), block_sum(rz)};
   if (last_block<2>(V.parts, m, &V.s->counter)) {
@@ -344,16 +428,26 @@ __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec
 
 template <int P>
 __global__ void __launch_bounds__(ST) k_pcg32_spmv(Grid g, int64_t nrows, PcgVec32 V) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   if (((volatile PcgScal*)V.s)->done) return;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
   float pq = 0.0f;
-  if (n < nrows) {
-    int ix, iy, iz;
-    decompose(g, n, ix, iy, iz);
-    RowInfo R = row_info(g, ix, iy, iz);
-    float q = row_apply_f<P>(g, R, V.J + R.rp, V.p);
-    V.q[n] = q;
-    pq = V.p[n] * q;
+  const int64_t ntiles = (nrows + ST - 1) / ST;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t n = tile * ST + threadIdx.x;
+    const bool act = n < nrows;
+    RowInfo R{};
+    if (act) {
+      int ix, iy, iz;
+      decompose(g, n, ix, iy, iz);
+      R = row_info(g, ix, iy, iz);
+    }
+    const float* vals = stage_rows<P, float>(g, nrows, V.J, R.rp, smem_raw, tile);
+    if (act) {
+      float q = row_apply_f<P>(g, R, vals, V.p);
+      V.q[n] = q;
+      pq = fmaf(V.p[n], q, pq);
+    }
+    if (P == 1) __syncthreads();
   }
   double m[1] = {block_sum((double)pq)};
   if (last_block<1>(V.parts, m, &V.s->counter)) {
@@ -370,17 +464,16 @@ __global__ void __launch_bounds__(ST) k_pcg32_spmv(Grid g, int64_t nrows, PcgVec
 
 __global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) {
   if (((volatile PcgScal*)V.s)->done) return;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
   const float alpha = (float)V.s->alpha;
   float rr = 0.0f, rz = 0.0f;
-  if (n < nrows) {
+  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
     V.x[n] = fmaf(alpha, V.p[n], V.x[n]);
     float r = fmaf(-alpha, V.q[n], V.r[n]);
     float z = r * V.minv[n];
     V.r[n] = r;
     V.z[n] = z;
-    rr = r * r;
-    rz = r * z;
+    rr = fmaf(r, r, rr);
+    rz = fmaf(r, z, rz);
   }
   double m[2] = {block_sum((double)rr), block_sum((double)rz)};
   if (last_block<2>(V.parts, m, &V.s->counter)) {
@@ -401,8 +494,9 @@ __global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) 
 
 __global__ void __launch_bounds__(ST) k_pcg32_dir(int64_t nrows, PcgVec32 V) {
   if (((volatile PcgScal*)V.s)->done) return;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
-  if (n < nrows) V.p[n] = fmaf((float)V.s->beta, V.p[n], V.z[n]);
+  const float beta = (float)V.s->beta;
+  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST)
+    V.p[n] = fmaf(beta, V.p[n], V.z[n]);
 }
 
 // u += (double) du32   (mixed path update; Dirichlet rows have du = 0 because r = 0 there)
@@ -421,13 +515,15 @@ __global__ void k_f32_to_f64(int64_t n, const float* __restrict__ a, double* __r
 
 // inf-norm with the last-block pattern; result in s->rnorm
 __global__ void __launch_bounds__(ST) k_norminf(int64_t n, const double* __restrict__ v, double* parts, PcgScal* s) {
-  int64_t i = (int64_t)blockIdx.x * ST + threadIdx.x;
-  double a = (i < n) ? fabs(v[i]) : 0.0;
-  if (i < n && !isfinite(v[i])) a = INFINITY;
+  double a = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * ST + threadIdx.x; i < n; i += (int64_t)gridDim.x * ST) {
+    const double x = v[i];
+    a = isfinite(x) ? fmax(a, fabs(x)) : INFINITY;
+  }
   double m[1] = {block_max(a)};
   if (last_block<1>(parts, m, &s->counter)) {
     double mx = 0.0;
-    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) mx = fmax(mx, ((volatile double*)parts)[k]);
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) mx = fmax(mx, __ldcg(parts + k));
     mx = block_max(mx);
     if (threadIdx.x == 0) {
       s->rnorm = mx;
@@ -437,6 +533,19 @@ __global__ void __launch_bounds__(ST) k_norminf(int64_t n, const double* __restr
 }
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// grid of the PCG kernels: one CTA per 128-row tile, at most 8 CTAs per SM
+inline unsigned pcg_grid(const mrg_problem* p) {
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
+  }
+  const unsigned tiles = nblk(p->ndof, ST);
+  const unsigned cap = (unsigned)(8 * nsm);
+  return tiles < cap ? tiles : cap;
+}
 
 }  // namespace
 
@@ -464,16 +573,17 @@ void mrg_solver_free(mrg_problem* p) {
   if (!w) return;
   if (w->g64) cudaGraphExecDestroy(w->g64);
   if (w->g32) cudaGraphExecDestroy(w->g32);
-  cudaFree(w->r); cudaFree(w->z); cudaFree(w->p); cudaFree(w->q); cudaFree(w->minv); cudaFree(w->parts);
-  cudaFree(w->x32); cudaFree(w->r32); cudaFree(w->z32); cudaFree(w->p32); cudaFree(w->q32); cudaFree(w->minv32);
-  cudaFree(w->s);
-  if (w->h_s) cudaFreeHost(w->h_s);
-  cudaFree(w->F); cudaFree(w->du); cudaFree(w->J64); cudaFree(w->J32);
+  cudaStream_t s = p->stream;
+  for (void* ptr : {(void*)w->r, (void*)w->z, (void*)w->p, (void*)w->q, (void*)w->minv, (void*)w->parts,
+                    (void*)w->x32, (void*)w->r32, (void*)w->z32, (void*)w->p32, (void*)w->q32, (void*)w->minv32,
+                    (void*)w->s, (void*)w->F, (void*)w->du, (void*)w->J64, (void*)w->J32})
+    if (ptr) cudaFreeAsync(ptr, s);
+  delete w->h_s;
   delete w;
   p->work = nullptr;
 }
 
-static int ensure_work(mrg_problem* p, bool need64, bool need32) {
+static int ensure_work(mrg_problem* p, bool need64, bool need32, cudaStream_t st) {
   if (!p->work) {
     p->work = new SolverWork();
     p->work->n = p->ndof;
@@ -482,44 +592,44 @@ static int ensure_work(mrg_problem* p, bool need64, bool need32) {
   SolverWork* w = p->work;
   const int64_t n = p->ndof;
   const size_t nparts = 3 * (size_t)nblk(n, ST) + 64;
-  if (!w->parts) MRG_CUDA(cudaMalloc(&w->parts, nparts * sizeof(double)));
+  if (!w->parts) MRG_CUDA(cudaMallocAsync(&w->parts, nparts * sizeof(double), st));
   if (!w->s) {
-    MRG_CUDA(cudaMalloc(&w->s, sizeof(PcgScal)));
-    MRG_CUDA(cudaMemset(w->s, 0, sizeof(PcgScal)));
-    MRG_CUDA(cudaMallocHost(&w->h_s, sizeof(PcgScal)));
+    MRG_CUDA(cudaMallocAsync(&w->s, sizeof(PcgScal), st));
+    MRG_CUDA(cudaMemsetAsync(w->s, 0, sizeof(PcgScal), st));
+    w->h_s = new PcgScal();
   }
   if (need64 && !w->r) {
-    MRG_CUDA(cudaMalloc(&w->r, n * sizeof(double)));
-    MRG_CUDA(cudaMalloc(&w->z, n * sizeof(double)));
-    MRG_CUDA(cudaMalloc(&w->p, n * sizeof(double)));
-    MRG_CUDA(cudaMalloc(&w->q, n * sizeof(double)));
-    MRG_CUDA(cudaMalloc(&w->minv, n * sizeof(double)));
+    MRG_CUDA(cudaMallocAsync(&w->r, n * sizeof(double), st));
+    MRG_CUDA(cudaMallocAsync(&w->z, n * sizeof(double), st));
+    MRG_CUDA(cudaMallocAsync(&w->p, n * sizeof(double), st));
+    MRG_CUDA(cudaMallocAsync(&w->q, n * sizeof(double), st));
+    MRG_CUDA(cudaMallocAsync(&w->minv, n * sizeof(double), st));
   }
   if (need32 && !w->r32) {
-    MRG_CUDA(cudaMalloc(&w->x32, n * sizeof(float)));
-    MRG_CUDA(cudaMalloc(&w->r32, n * sizeof(float)));
-    MRG_CUDA(cudaMalloc(&w->z32, n * sizeof(float)));
-    MRG_CUDA(cudaMalloc(&w->p32, n * sizeof(float)));
-    MRG_CUDA(cudaMalloc(&w->q32, n * sizeof(float)));
-    MRG_CUDA(cudaMalloc(&w->minv32, n * sizeof(float)));
+    MRG_CUDA(cudaMallocAsync(&w->x32, n * sizeof(float), st));
+    MRG_CUDA(cudaMallocAsync(&w->r32, n * sizeof(float), st));
+    MRG_CUDA(cudaMallocAsync(&w->z32, n * sizeof(float), st));
+    MRG_CUDA(cudaMallocAsync(&w->p32, n * sizeof(float), st));
+    MRG_CUDA(cudaMallocAsync(&w->q32, n * sizeof(float), st));
+    MRG_CUDA(cudaMallocAsync(&w->minv32, n * sizeof(float), st));
   }
   return MRG_OK;
 }
 
 template <int P>
 static void enqueue_chunk64(const mrg_problem* p, const PcgVec64& V, cudaStream_t s) {
-  const unsigned nb = nblk(p->ndof, ST);
+  const unsigned nb = pcg_grid(p);
   for (int it = 0; it < CHUNK; ++it) {
-    k_pcg64_spmv<P><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+    k_pcg64_spmv<P><<<nb, ST, stage_bytes<P, double>(), s>>>(p->g, p->ndof, V);
     k_pcg64_update<<<nb, ST, 0, s>>>(p->ndof, V);
     k_pcg64_dir<<<nb, ST, 0, s>>>(p->ndof, V);
   }
 }
 template <int P>
 static void enqueue_chunk32(const mrg_problem* p, const PcgVec32& V, cudaStream_t s) {
-  const unsigned nb = nblk(p->ndof, ST);
+  const unsigned nb = pcg_grid(p);
   for (int it = 0; it < CHUNK; ++it) {
-    k_pcg32_spmv<P><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
+    k_pcg32_spmv<P><<<nb, ST, stage_bytes<P, float>(), s>>>(p->g, p->ndof, V);
     k_pcg32_update<<<nb, ST, 0, s>>>(p->ndof, V);
     k_pcg32_dir<<<nb, ST, 0, s>>>(p->ndof, V);
   }
@@ -574,7 +684,7 @@ static int run_chunks(mrg_problem* p, cudaGraphExec_t exec, cudaStream_t s, int 
 
 static int pcg64(mrg_problem* p, const double* J, const double* b, double* x, double rtol, int maxiter,
                  mrg_solve_stats* st, cudaStream_t s) {
-  int rc = ensure_work(p, true, false);
+  int rc = ensure_work(p, true, false, s);
   if (rc) return rc;
   SolverWork* w = p->work;
   PcgVec64 V{x, w->r, w->z, w->p, w->q, w->minv, w->parts, b, J, w->s};
@@ -582,7 +692,7 @@ static int pcg64(mrg_problem* p, const double* J, const double* b, double* x, do
   init.tol = rtol;
   init.maxiter = maxiter;
   MRG_CUDA(cudaMemcpyAsync(w->s, &init, sizeof(PcgScal), cudaMemcpyHostToDevice, s));
-  const unsigned nb = nblk(p->ndof, ST);
+  const unsigned nb = pcg_grid(p);
   if (p->g.p == 1) k_pcg64_init<1><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
   else k_pcg64_init<2><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
   MRG_CUDA(cudaGetLastError());
@@ -609,7 +719,7 @@ static int pcg64(mrg_problem* p, const double* J, const double* b, double* x, do
 // FP32 PCG on J32 dx = b (x0 = 0); result in w->x32
 static int pcg32(mrg_problem* p, const float* J, const double* b, double rtol, int maxiter, mrg_solve_stats* st,
                  cudaStream_t s) {
-  int rc = ensure_work(p, false, true);
+  int rc = ensure_work(p, false, true, s);
   if (rc) return rc;
   SolverWork* w = p->work;
   PcgVec32 V{w->x32, w->r32, w->z32, w->p32, w->q32, w->minv32, w->parts, b, J, w->s};
@@ -617,7 +727,7 @@ static int pcg32(mrg_problem* p, const float* J, const double* b, double rtol, i
   init.tol = rtol;
   init.maxiter = maxiter;
   MRG_CUDA(cudaMemcpyAsync(w->s, &init, sizeof(PcgScal), cudaMemcpyHostToDevice, s));
-  const unsigned nb = nblk(p->ndof, ST);
+  const unsigned nb = pcg_grid(p);
   if (p->g.p == 1) k_pcg32_init<1><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
   else k_pcg32_init<2><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
   MRG_CUDA(cudaGetLastError());
@@ -642,8 +752,8 @@ extern "C" int mrg_spmv(const mrg_problem* p, const void* J, int32_t fp32, const
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned nb = nblk(p->ndof, ST);
   if (p->g.p == 1) {
-    if (fp32) k_spmv<1, float><<<nb, ST, 0, s>>>(p->g, p->ndof, (const float*)J, x, y);
-    else k_spmv<1, double><<<nb, ST, 0, s>>>(p->g, p->ndof, (const double*)J, x, y);
+    if (fp32) k_spmv<1, float><<<nb, ST, stage_bytes<1, float>(), s>>>(p->g, p->ndof, (const float*)J, x, y);
+    else k_spmv<1, double><<<nb, ST, stage_bytes<1, double>(), s>>>(p->g, p->ndof, (const double*)J, x, y);
   } else {
     if (fp32) k_spmv<2, float><<<nb, ST, 0, s>>>(p->g, p->ndof, (const float*)J, x, y);
     else k_spmv<2, double><<<nb, ST, 0, s>>>(p->g, p->ndof, (const double*)J, x, y);
@@ -657,9 +767,10 @@ extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const 
   if (!p || !J || !b || !x) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg: null argument");
   if (!(rtol >= 0.0) || maxiter < 0) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg: bad tolerance or iteration limit");
   cudaStream_t s = (cudaStream_t)stream;
+  p->last_stream = s;
   if (!fp32) return pcg64(p, (const double*)J, b, x, rtol, maxiter, st, s);
   // FP32 matrix: solve J dx = b - J x0 in FP32, then x = x0 + dx
-  int rc = ensure_work(p, true, true);
+  int rc = ensure_work(p, true, true, s);
   if (rc) return rc;
   SolverWork* w = p->work;
   double* res = w->r;  // b - J x0
@@ -680,7 +791,7 @@ extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const 
 
 static int norm_inf(mrg_problem* p, const double* v, double* out, cudaStream_t s) {
   SolverWork* w = p->work;
-  k_norminf<<<nblk(p->ndof, ST), ST, 0, s>>>(p->ndof, v, w->parts, w->s);
+  k_norminf<<<pcg_grid(p), ST, 0, s>>>(p->ndof, v, w->parts, w->s);
   MRG_CUDA(cudaGetLastError());
   MRG_CUDA(cudaMemcpyAsync(w->h_s, w->s, sizeof(PcgScal), cudaMemcpyDeviceToHost, s));
   MRG_CUDA(cudaStreamSynchronize(s));
@@ -693,16 +804,17 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
   if (!p || !u || !o) return mrg_fail(MRG_EINVAL, "mrg_newton: null argument");
   if (o->max_iters < 1 || !(o->nl_tol > 0.0)) return mrg_fail(MRG_EINVAL, "mrg_newton: bad options");
   cudaStream_t s = (cudaStream_t)stream;
+  p->last_stream = s;
   const bool mixed = o->mixed != 0;
-  int rc = ensure_work(p, true, mixed);
+  int rc = ensure_work(p, true, mixed, s);
   if (rc) return rc;
   SolverWork* w = p->work;
   if (!w->F) {
-    MRG_CUDA(cudaMalloc(&w->F, p->ndof * sizeof(double)));
-    MRG_CUDA(cudaMalloc(&w->du, p->ndof * sizeof(double)));
+    MRG_CUDA(cudaMallocAsync(&w->F, p->ndof * sizeof(double), s));
+    MRG_CUDA(cudaMallocAsync(&w->du, p->ndof * sizeof(double), s));
   }
-  if (mixed && !w->J32) MRG_CUDA(cudaMalloc(&w->J32, p->nnz * sizeof(float)));
-  if (!mixed && !w->J64) MRG_CUDA(cudaMalloc(&w->J64, p->nnz * sizeof(double)));
+  if (mixed && !w->J32) MRG_CUDA(cudaMallocAsync(&w->J32, p->nnz * sizeof(float), s));
+  if (!mixed && !w->J64) MRG_CUDA(cudaMallocAsync(&w->J64, p->nnz * sizeof(double), s));
   void* J = mixed ? (void*)w->J32 : (void*)w->J64;
   const uint32_t jflags = MRG_ASM_JAC | MRG_ASM_OVERWRITE | (mixed ? MRG_ASM_J_FP32 : 0u);
   rc = mrg_set_dirichlet(p, u, stream);
@@ -848,7 +960,7 @@ extern "C" int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J, const doub
   cudaStream_t s = (cudaStream_t)stream;
   PcgVec64 V{x, S->vec[0], S->vec[1], S->vec[2], S->vec[3], S->vec[4], S->parts, b, J, &S->scal};
   k_na_init_scal<<<1, 1, 0, s>>>(&S->scal, rtol, maxiter);
-  const unsigned nb = nblk(p->ndof, ST);
+  const unsigned nb = pcg_grid(p);
   if (p->g.p == 1) k_pcg64_init<1><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
   else k_pcg64_init<2><<<nb, ST, 0, s>>>(p->g, p->ndof, V);
   MRG_CUDA(cudaGetLastError());
