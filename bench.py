@@ -335,6 +335,14 @@ def run_ours(args, rank, world, local_rank):
         sol["mixed_speedup_e2e"] = sol["fp64"]["seconds"] / sol["mixed"]["seconds"]
         out["solve"] = sol
 
+    if not args.no_extras:
+        for name, fn in (("c3", bench_c3), ("c4", bench_c4), ("c5", bench_c5)):
+            try:
+                out[name] = fn(args)
+            except Exception as e:  # reported, never fatal for the headline line
+                out[name] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.synchronize()
+
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline()
@@ -342,6 +350,115 @@ def run_ours(args, rank, world, local_rank):
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def _ev_time(fn, reps):
+    import torch
+
+    s = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    a.record(s)
+    for _ in range(reps):
+        fn()
+    b.record(s)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def bench_c3(args):
+    """C3: -div((1+u^2) grad u) = 10 on 64^3 Q2 hexes, u0 ~ U(0, 0.1); Newton to 1e-10 (mixed: FP32
+    Jacobian + FP32 inner PCG, FP64 residual), plus per-assembly timings."""
+    import torch
+
+    from mrhyde_gb300 import AssemblyManager, Problem, SolverManager
+    from mrhyde_gb300.workloads import c3
+
+    cfg, u0 = c3(seed=3, n=args.c3_n)
+    P = Problem(**cfg)
+    A = AssemblyManager(P)
+    info = P.info
+    u = torch.tensor(u0, device="cuda")
+    r = P.new_vector()
+    J32 = P.new_matrix_values(fp32=True)
+    t_res = _ev_time(lambda: A.assembleRes(u, r, overwrite=True), 5)
+    t_j32 = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True), 3)
+    out = {"workload": f"{args.c3_n}^3 Q2 hex, 27 nodes/cell, 3x3x3 Gauss, u=0 on x=0,1", "cells": info.n_cells,
+           "dofs": info.n_dofs, "nnz": info.nnz,
+           "residual_fp64_ms": t_res, "residual_cells_per_s": info.n_cells / (t_res * 1e-3),
+           "jac_fp32_plus_res_ms": t_j32, "jac_fp32_cells_per_s": info.n_cells / (t_j32 * 1e-3)}
+    del J32
+    torch.cuda.empty_cache()
+    S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=25, linear_tol=1e-3, linear_maxiter=20000,
+                      mixed_precision=True)
+    uu = torch.tensor(u0, device="cuda")
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    res = S.nonlinearSolver(uu, raise_on_noconv=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    out["newton_mixed"] = {"seconds": dt, "newton_iters": res.outer_iterations, "pcg_iters": res.iterations,
+                           "rel_residual_inf": res.rel_residual, "cells_per_s": info.n_cells / dt,
+                           "dof_per_s": info.n_dofs / dt}
+    return out
+
+
+def bench_c4(args):
+    """C4: 4096 local steady-thermal problems (per-axis cells U{4..16}), one persistent launch."""
+    import torch
+
+    from mrhyde_gb300.subgrid import SubgridBatch
+    from mrhyde_gb300.workloads import c4_problem, c4_sizes
+
+    sizes = c4_sizes(4096, seed=4)
+    probs = [c4_problem(sizes, k, seed=4) for k in range(len(sizes))]
+    B = SubgridBatch(sizes, [p["kappa"] for p in probs], [p["dirichlet"][1] for p in probs], source=1.0)
+    cfg = B.autotune()
+    st = B.solve()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s = torch.cuda.current_stream()
+    reps = 3
+    a.record(s)
+    for _ in range(reps):
+        B.solve(stats=False)
+    b.record(s)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    st = B.solve()
+    info = B.info
+    return {"problems": int(len(sizes)), "cells": int(info.n_cells), "dofs": int(info.n_nodes), "nnz": int(info.nnz),
+            "ms_per_batch": ms, "cells_per_s": info.n_cells / (ms * 1e-3), "dof_per_s": info.n_nodes / (ms * 1e-3),
+            "problems_per_s": len(sizes) / (ms * 1e-3), "config": {"threads": cfg[0], "ctas_per_sm": cfg[1]},
+            "max_rel_residual": float(st[:, 2].max()), "mean_outer": float(st[:, 0].mean()),
+            "mean_inner": float(st[:, 1].mean()), "all_converged": bool((st[:, 3] == 0).all())}
+
+
+def bench_c5(args):
+    """C5: Poisson stream (200 req/s) of thermal and nonlinear-diffusion solves on Q1 cubes with edge
+    log-uniform in [16, 96], admitted under an 80 GB budget; p50/p99 latency and DOF/s, mixed vs FP64;
+    plus the batch throughput (all requests at t=0) and a stream at 80 % of it."""
+    from mrhyde_gb300 import serving
+
+    out = {}
+    for mode in ("mixed", "fp64"):
+        reqs = serving.poisson_stream(rate=200.0, count=args.c5_count, mixed=(mode == "mixed"), seed=5)
+        srv = serving.Server(hbm_budget_bytes=80 * 10**9, slots=args.c5_slots)
+        out[mode] = srv.run(reqs, realtime=True)
+        out[mode]["peak_active"] = srv.peak_active
+    reqs = serving.poisson_stream(rate=200.0, count=args.c5_count, mixed=True, seed=5)
+    batch = serving.Server(hbm_budget_bytes=80 * 10**9, slots=args.c5_slots).run(reqs, realtime=False)
+    out["batch_mixed"] = batch
+    rate80 = 0.8 * batch["req_per_s"]
+    reqs = serving.poisson_stream(rate=rate80, count=args.c5_count, mixed=True, seed=6)
+    s80 = serving.Server(hbm_budget_bytes=80 * 10**9, slots=args.c5_slots).run(reqs, realtime=True)
+    s80["rate"] = rate80
+    s80["p99_over_p50"] = s80["p99_ms"] / s80["p50_ms"]
+    out["stream_at_80pct_batch"] = s80
+    out["config"] = {"arrivals": "Poisson 200/s", "edge": "log-uniform [16,96]", "nonlinear_fraction": 0.5,
+                     "kappa": "lognormal sigma=1 per cell (device generator, per-request seed)",
+                     "budget_bytes": 80 * 10**9, "slots": args.c5_slots, "requests": args.c5_count}
+    return out
 
 
 def run_profile(args, local_rank):
@@ -383,6 +500,10 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the C3/C4/C5 measurements")
+    ap.add_argument("--c3-n", type=int, default=64)
+    ap.add_argument("--c5-count", type=int, default=400)
+    ap.add_argument("--c5-slots", type=int, default=12)
     ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()

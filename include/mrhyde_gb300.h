@@ -105,7 +105,8 @@ typedef struct mrg_problem_info {
 enum {
   MRG_PATH_FACTORED = 1,   /* identical affine cells: K_e = kappa_c * K_ref, row-gather assembly */
   MRG_PATH_CELL = 2,       /* per-cell geometry + forward-AD tangents in registers, colored scatter */
-  MRG_PATH_Q2_TC = 3       /* Q2 hexahedra: element contractions on tensor cores (tcgen05) */
+  MRG_PATH_TENSOR = 3      /* identical affine hexahedra, Q2 or nonlinear Q1: sum-factorised FP64 residual,
+                              row-gather Jacobian (each (row, cell) pair one row of a constant-operand GEMM) */
 };
 
 /* mrg_assemble flags */
@@ -118,7 +119,8 @@ enum {
   MRG_ASM_FORCE_CELL = 256u,   /* force the per-cell AD path (testing)           */
   MRG_ASM_ATOMIC = 512u,       /* per-cell path: atomic scatter instead of 8-colour scatter */
   MRG_ASM_ADJOINT = 1024u,     /* not supported -> MRG_ENOTSUP                   */
-  MRG_ASM_SENS = 2048u         /* not supported -> MRG_ENOTSUP                   */
+  MRG_ASM_SENS = 2048u,        /* not supported -> MRG_ENOTSUP                   */
+  MRG_ASM_TENSOR_CORES = 4096u /* Q2 FP32 Jacobian: element contractions on tcgen05 tensor cores (3xTF32) */
 };
 
 /* ---- problem lifetime ------------------------------------------------------------------------- */

@@ -19,7 +19,7 @@ MRG_SRC_CONST, MRG_SRC_SINPROD = 0, 1
 MRG_DBC_CONST, MRG_DBC_NODE = 0, 1
 MRG_FACE_XLO, MRG_FACE_XHI, MRG_FACE_YLO, MRG_FACE_YHI, MRG_FACE_ZLO, MRG_FACE_ZHI = 1, 2, 4, 8, 16, 32
 MRG_FACE_ALL = 63
-MRG_PATH_FACTORED, MRG_PATH_CELL, MRG_PATH_Q2_TC = 1, 2, 3
+MRG_PATH_FACTORED, MRG_PATH_CELL, MRG_PATH_TENSOR = 1, 2, 3
 
 MRG_ASM_RES = 1
 MRG_ASM_JAC = 2
@@ -30,6 +30,7 @@ MRG_ASM_FORCE_CELL = 256
 MRG_ASM_ATOMIC = 512
 MRG_ASM_ADJOINT = 1024
 MRG_ASM_SENS = 2048
+MRG_ASM_TENSOR_CORES = 4096
 MRG_NOALLOC_MAX_DOFS = 1 << 18
 
 

@@ -429,6 +429,7 @@ struct CellArgs {
   int npe, nq, nvpe;
   int kind, src_sin;
   double amp, freq;
+  double lo[3], h[3];  // uniform box geometry when vcoord == nullptr
   int color;        // -1: all cells (atomic scatter)
   int cc[3];        // cells of this colour per axis
   int64_t ncells_launch;
@@ -487,9 +488,15 @@ __global__ void __launch_bounds__(CPB*(P + 1) * (P + 1) * (DIM == 3 ? P + 1 : 1)
     }
     for (int v = t; v < NV; v += NPE) {
       int a = v % 2, b = (v / 2) % 2, c = (DIM == 3) ? v / 4 : 0;
-      int64_t vid = (cx + a) + (int64_t)(g.nc[0] + 1) * ((cy + b) + (int64_t)(g.nc[1] + 1) * (cz + c));
+      if (A.vcoord) {
+        int64_t vid = (cx + a) + (int64_t)(g.nc[0] + 1) * ((cy + b) + (int64_t)(g.nc[1] + 1) * (cz + c));
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) s_x[slot][v][k] = __ldg(A.vcoord + vid * DIM + k);
+        for (int k = 0; k < DIM; ++k) s_x[slot][v][k] = __ldg(A.vcoord + vid * DIM + k);
+      } else {
+        const int iv[3] = {cx + a, cy + b, cz + c};
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) s_x[slot][v][k] = A.lo[k] + A.h[k] * iv[k];
+      }
     }
   }
   __syncthreads();
@@ -778,6 +785,10 @@ int mrg_launch_cell(mrg_problem* p, const double* u, double* r, void* J, uint32_
   A.tab.psi = A.tab.dphi + npe * nq * d;
   A.tab.dpsi = A.tab.psi + nv * nq;
   A.vcoord = p->d_vcoord;
+  for (int k = 0; k < 3; ++k) {
+    A.lo[k] = p->lo[k];
+    A.h[k] = p->h[k];
+  }
   A.npe = npe;
   A.nq = nq;
   A.nvpe = nv;

@@ -125,5 +125,8 @@ int mrg_launch_kappa32(mrg_problem* p, cudaStream_t s);
 int mrg_q2_setup(mrg_problem* p);
 void mrg_q2_free(mrg_problem* p);
 int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s);
+// Q2 Jacobian contractions on tcgen05 tensor cores (mrg_tc_q2.cu)
+int mrg_launch_q2_jac_tc(const mrg_problem* p, const float* tab32, const float* qbuf, float* J, bool ovw, int* err,
+                         double s0, double s1, double s2, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);

@@ -140,6 +140,11 @@ __global__ void k_dof_map(Grid g, int64_t ncell, int npe, int32_t* __restrict__ 
   lids[e] = (g.p * cx + a) + g.nn[0] * ((g.p * cy + b) + g.nn[1] * (g.p * cz + cc));
 }
 
+__global__ void k_fill(double* __restrict__ a, int64_t n, double v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
 __global__ void k_set_dirichlet(const int32_t* __restrict__ dofs, const double* __restrict__ vals, int64_t n,
                                 double* __restrict__ u) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -250,8 +255,9 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
   P->affine = (m->vertex_coords == nullptr);
   if (P->affine && p == 1 && ph->kind == MRG_THERMAL && qo >= 2)
     P->path = MRG_PATH_FACTORED;
-  else if (P->affine && p == 2 && m->dim == 3 && n1 == 3 && ph->source_kind == MRG_SRC_CONST)
-    P->path = MRG_PATH_Q2_TC;
+  else if (P->affine && m->dim == 3 && n1 == p + 1 && ph->source_kind == MRG_SRC_CONST &&
+           (p == 2 || ph->kind == MRG_DIFFUSION_1PU2))
+    P->path = MRG_PATH_TENSOR;
   else
     P->path = MRG_PATH_CELL;
 
@@ -267,29 +273,45 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
     return fail_cuda(e, "upload prefix");
   for (int k = 0; k < 3; ++k) g.P[k] = P->d_prefix + offs[k];
   // coefficients
-  std::vector<double> kap(P->ncell, ph->kappa_const);
-  if (ph->kappa_cell)
-    for (int64_t c = 0; c < P->ncell; ++c) kap[c] = ph->kappa_cell[c];
-  for (int64_t c = 0; c < P->ncell; ++c)
-    if (!std::isfinite(kap[c])) {
-      free_problem(P);
-      return mrg_fail(MRG_ENUMERIC, "kappa contains NaN or Inf");
-    }
+  if (ph->kappa_cell) {
+    for (int64_t c = 0; c < P->ncell; ++c)
+      if (!std::isfinite(ph->kappa_cell[c])) {
+        free_problem(P);
+        return mrg_fail(MRG_ENUMERIC, "kappa contains NaN or Inf");
+      }
+  } else if (!std::isfinite(ph->kappa_const)) {
+    free_problem(P);
+    return mrg_fail(MRG_ENUMERIC, "kappa contains NaN or Inf");
+  }
   if ((e = cudaMallocAsync(&P->d_kappa, P->ncell * sizeof(double), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc kappa");
   if ((e = cudaMallocAsync(&P->d_kappa32, P->ncell * sizeof(float), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc kappa32");
-  if ((e = cudaMemcpyAsync(P->d_kappa, kap.data(), P->ncell * sizeof(double), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
-    return fail_cuda(e, "upload kappa");
-  // Dirichlet DOFs in increasing order
+  if (ph->kappa_cell) {
+    if ((e = cudaMemcpyAsync(P->d_kappa, ph->kappa_cell, P->ncell * sizeof(double), cudaMemcpyHostToDevice, cs)) != cudaSuccess)
+      return fail_cuda(e, "upload kappa");
+  } else {
+    k_fill<<<nblk(P->ncell, 256), 256, 0, cs>>>(P->d_kappa, P->ncell, ph->kappa_const);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "fill kappa");
+  }
+  // Dirichlet DOFs in increasing order; only boundary rows of the node grid are visited
   std::vector<int32_t> fixed;
   std::vector<double> fvals;
+  auto add_fixed = [&](int ix, int iy, int iz) {
+    int32_t n = ix + g.nn[0] * (iy + g.nn[1] * iz);
+    fixed.push_back(n);
+    fvals.push_back(ph->dirichlet_kind == MRG_DBC_NODE ? ph->dirichlet_node[n] : ph->dirichlet_const);
+  };
   for (int iz = 0; iz < g.nn[2]; ++iz)
-    for (int iy = 0; iy < g.nn[1]; ++iy)
-      for (int ix = 0; ix < g.nn[0]; ++ix)
-        if (node_fixed(g, ix, iy, iz)) {
-          int32_t n = ix + g.nn[0] * (iy + g.nn[1] * iz);
-          fixed.push_back(n);
-          fvals.push_back(ph->dirichlet_kind == MRG_DBC_NODE ? ph->dirichlet_node[n] : ph->dirichlet_const);
+    for (int iy = 0; iy < g.nn[1]; ++iy) {
+      if (node_fixed(g, 1 % g.nn[0], iy, iz) && g.nn[0] > 2) {
+        // an interior x position is fixed: the whole x-line lies on a y or z face
+        for (int ix = 0; ix < g.nn[0]; ++ix) add_fixed(ix, iy, iz);
+      } else {
+        for (int ix = 0; ix < g.nn[0]; ++ix) {
+          if (ix > 0 && ix < g.nn[0] - 1) ix = g.nn[0] - 1;  // interior x positions are free on this line
+          if (node_fixed(g, ix, iy, iz)) add_fixed(ix, iy, iz);
         }
+      }
+    }
   P->nfixed = (int64_t)fixed.size();
   if (P->nfixed > 0) {
     if ((e = cudaMallocAsync(&P->d_fixed, P->nfixed * sizeof(int32_t), cs)) != cudaSuccess) return fail_cuda(e, "cudaMalloc fixed");
@@ -397,9 +419,9 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
         return fail_cuda(e, "upload srcB");
     }
   }
-  // vertex coordinates for the general path
+  // vertex coordinates for the general path (uniform boxes: computed in the kernel from lo and h)
   int64_t nvert = (int64_t)(g.nc[0] + 1) * (g.nc[1] + 1) * (d == 3 ? g.nc[2] + 1 : 1);
-  {
+  if (m->vertex_coords) {
     std::vector<double> vc(nvert * d);
     for (int64_t v = 0; v < nvert; ++v) {
       int iv[3] = {(int)(v % (g.nc[0] + 1)), (int)((v / (g.nc[0] + 1)) % (g.nc[1] + 1)),
@@ -413,7 +435,7 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
       return fail_cuda(e, "upload vcoord");
   }
   int st = mrg_launch_kappa32(P, cs);
-  if (st == MRG_OK && P->path == MRG_PATH_Q2_TC) st = mrg_q2_setup(P);
+  if (st == MRG_OK && P->path == MRG_PATH_TENSOR) st = mrg_q2_setup(P);
   if (st != MRG_OK) {
     free_problem(P);
     return st;
@@ -507,7 +529,7 @@ extern "C" int mrg_assemble(mrg_problem* p, const double* u, double* r, void* J,
   if (p->path == MRG_PATH_FACTORED && !(flags & MRG_ASM_FORCE_CELL)) {
     st = mrg_launch_factored(p, u, r, J, flags, s);
     if (st != MRG_OK) return st;
-  } else if (p->path == MRG_PATH_Q2_TC && !(flags & MRG_ASM_FORCE_CELL)) {
+  } else if (p->path == MRG_PATH_TENSOR && !(flags & MRG_ASM_FORCE_CELL)) {
     st = mrg_launch_q2(p, u, r, J, flags, s);
     if (st != MRG_OK) return st;
   } else {

@@ -115,6 +115,42 @@ constexpr int stage_bytes() {
   return P == 1 ? (ST * 27 + 16 / (int)sizeof(JT)) * (int)sizeof(JT) : 0;
 }
 
+// Double-buffered staging for the PCG SpMV (P = 1): tile t's CSR segment is copied into shared
+// memory with cp.async (16-byte, L2-only) while tile t - G is being multiplied.  The ragged head and
+// tail of a segment (not 16-byte aligned) are copied with plain loads.
+constexpr int STAGE_ELEMS_PAD = 4;
+template <typename JT>
+constexpr int stage_elems() { return ST * 27 + STAGE_ELEMS_PAD; }
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// issues the copy of `tile`'s segment into buf; returns seg0
+template <typename JT>
+__device__ __forceinline__ int64_t tile_issue(const Grid& g, int64_t nrows, const JT* __restrict__ J, int64_t tile,
+                                              JT* buf) {
+  const int64_t n0 = tile * ST;
+  const int64_t n1 = (n0 + ST < nrows) ? n0 + ST : nrows;
+  const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
+  const JT* src = J + seg0;
+  JT* dst = buf + (int)(((uintptr_t)src & 15) / sizeof(JT));
+  const int64_t len = seg1 - seg0;
+  constexpr int V = 16 / sizeof(JT);
+  int head = (int)(((16 - ((uintptr_t)src & 15)) & 15) / sizeof(JT));
+  if (head > len) head = (int)len;
+  const int64_t body = (len - head) / V;
+  for (int k = threadIdx.x; k < head; k += blockDim.x) dst[k] = __ldcs(src + k);
+  for (int64_t v = threadIdx.x; v < body; v += blockDim.x) cp_async16(dst + head + v * V, src + head + v * V);
+  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) dst[k] = __ldcs(src + k);
+  cp_async_commit();
+  return seg0;
+}
+
 // sum of v over the block, returned in thread 0 (FP64)
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double sh[32];
@@ -192,6 +228,17 @@ __device__ __forceinline__ double row_apply(const Grid& g, const RowInfo& R, con
                                             const XT* __restrict__ x) {
   constexpr int MC = 2 * P + 1;
   const int64_t NX = g.nn[0], plane = (int64_t)g.nn[0] * g.nn[1];
+  if (P == 1 && R.cx == 3 && R.cy == 3 && R.cz == 3) {
+    // interior row: all 27 couplings, no predicates, so all loads issue before the FMAs
+    const XT* xb = x + R.lx + NX * R.ly + plane * R.lz;
+    double xv[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) xv[k] = (double)__ldg(xb + (k % 3) + NX * ((k / 3) % 3) + plane * (k / 9));
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < 27; ++k) acc = fma((double)vals[k], xv[k], acc);
+    return acc;
+  }
   double acc = 0.0;
   int pos = 0;
 #pragma unroll
@@ -220,6 +267,16 @@ __device__ __forceinline__ float row_apply_f(const Grid& g, const RowInfo& R, co
                                              const float* __restrict__ x) {
   constexpr int MC = 2 * P + 1;
   const int64_t NX = g.nn[0], plane = (int64_t)g.nn[0] * g.nn[1];
+  if (P == 1 && R.cx == 3 && R.cy == 3 && R.cz == 3) {
+    const float* xb = x + R.lx + NX * R.ly + plane * R.lz;
+    float xv[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) xv[k] = __ldg(xb + (k % 3) + NX * ((k / 3) % 3) + plane * (k / 9));
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 27; ++k) acc = fmaf(vals[k], xv[k], acc);
+    return acc;
+  }
   float acc = 0.0f;
   int pos = 0;
 #pragma unroll
@@ -312,22 +369,43 @@ __global__ void __launch_bounds__(ST) k_pcg64_spmv(Grid g, int64_t nrows, PcgVec
   if (((volatile PcgScal*)V.s)->done) return;
   double pq = 0.0;
   const int64_t ntiles = (nrows + ST - 1) / ST;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t n = tile * ST + threadIdx.x;
-    const bool act = n < nrows;
-    RowInfo R{};
-    if (act) {
+  if constexpr (P == 1) {
+    double* bufs[2] = {reinterpret_cast<double*>(smem_raw), reinterpret_cast<double*>(smem_raw) + stage_elems<double>()};
+    int64_t seg[2] = {0, 0};
+    int b = 0;
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles) seg[0] = tile_issue<double>(g, nrows, V.J, tile, bufs[0]);
+    for (; tile < ntiles; tile += gridDim.x) {
+      const int64_t nxt = tile + gridDim.x;
+      if (nxt < ntiles) {
+        seg[b ^ 1] = tile_issue<double>(g, nrows, V.J, nxt, bufs[b ^ 1]);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+      const int64_t n = tile * ST + threadIdx.x;
+      if (n < nrows) {
+        int ix, iy, iz;
+        decompose(g, n, ix, iy, iz);
+        const RowInfo R = row_info(g, ix, iy, iz);
+        const double* sv = bufs[b] + (int)(((uintptr_t)(V.J + seg[b]) & 15) / sizeof(double));
+        const double q = row_apply<1, double, double>(g, R, sv + (R.rp - seg[b]), V.p);
+        V.q[n] = q;
+        pq = fma(V.p[n], q, pq);
+      }
+      __syncthreads();
+      b ^= 1;
+    }
+  } else {
+    for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
       int ix, iy, iz;
       decompose(g, n, ix, iy, iz);
-      R = row_info(g, ix, iy, iz);
-    }
-    const double* vals = stage_rows<P, double>(g, nrows, V.J, R.rp, smem_raw, tile);
-    if (act) {
-      double q = row_apply<P, double, double>(g, R, vals, V.p);
+      const RowInfo R = row_info(g, ix, iy, iz);
+      const double q = row_apply<P, double, double>(g, R, V.J + R.rp, V.p);
       V.q[n] = q;
       pq = fma(V.p[n], q, pq);
     }
-    if (P == 1) __syncthreads();  // the next tile reuses the staging buffer
   }
   double m[1] = {block_sum(pq)};
   if (last_block<1>(V.parts, m, &V.s->counter)) {
@@ -347,7 +425,27 @@ __global__ void __launch_bounds__(ST) k_pcg64_update(int64_t nrows, PcgVec64 V) 
   if (((volatile PcgScal*)V.s)->done) return;
   const double alpha = V.s->alpha;
   double rr = 0.0, rz = 0.0;
-  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
+  const int64_t st = (int64_t)gridDim.x * ST;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  for (; n + 3 * st < nrows; n += 4 * st) {
+    double p[4], q[4], r[4], x[4], mi[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      p[k] = V.p[n + k * st]; q[k] = V.q[n + k * st]; r[k] = V.r[n + k * st];
+      x[k] = V.x[n + k * st]; mi[k] = V.minv[n + k * st];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      V.x[n + k * st] = fma(alpha, p[k], x[k]);
+      const double rn = fma(-alpha, q[k], r[k]);
+      const double z = rn * mi[k];
+      V.r[n + k * st] = rn;
+      V.z[n + k * st] = z;
+      rr = fma(rn, rn, rr);
+      rz = fma(rn, z, rz);
+    }
+  }
+  for (; n < nrows; n += st) {
     V.x[n] = fma(alpha, V.p[n], V.x[n]);
     double r = fma(-alpha, V.q[n], V.r[n]);
     double z = r * V.minv[n];
@@ -377,8 +475,16 @@ __global__ void __launch_bounds__(ST) k_pcg64_update(int64_t nrows, PcgVec64 V) 
 __global__ void __launch_bounds__(ST) k_pcg64_dir(int64_t nrows, PcgVec64 V) {
   if (((volatile PcgScal*)V.s)->done) return;
   const double beta = V.s->beta;
-  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST)
-    V.p[n] = fma(beta, V.p[n], V.z[n]);
+  const int64_t st = (int64_t)gridDim.x * ST;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  for (; n + 3 * st < nrows; n += 4 * st) {
+    double p[4], z[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { p[k] = V.p[n + k * st]; z[k] = V.z[n + k * st]; }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) V.p[n + k * st] = fma(beta, p[k], z[k]);
+  }
+  for (; n < nrows; n += st) V.p[n] = fma(beta, V.p[n], V.z[n]);
 }
 
 // ---- FP32 inner PCG kernels (mixed path) ---------------------------------------------------------
@@ -432,22 +538,43 @@ __global__ void __launch_bounds__(ST) k_pcg32_spmv(Grid g, int64_t nrows, PcgVec
   if (((volatile PcgScal*)V.s)->done) return;
   float pq = 0.0f;
   const int64_t ntiles = (nrows + ST - 1) / ST;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t n = tile * ST + threadIdx.x;
-    const bool act = n < nrows;
-    RowInfo R{};
-    if (act) {
+  if constexpr (P == 1) {
+    float* bufs[2] = {reinterpret_cast<float*>(smem_raw), reinterpret_cast<float*>(smem_raw) + stage_elems<float>()};
+    int64_t seg[2] = {0, 0};
+    int b = 0;
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles) seg[0] = tile_issue<float>(g, nrows, V.J, tile, bufs[0]);
+    for (; tile < ntiles; tile += gridDim.x) {
+      const int64_t nxt = tile + gridDim.x;
+      if (nxt < ntiles) {
+        seg[b ^ 1] = tile_issue<float>(g, nrows, V.J, nxt, bufs[b ^ 1]);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+      const int64_t n = tile * ST + threadIdx.x;
+      if (n < nrows) {
+        int ix, iy, iz;
+        decompose(g, n, ix, iy, iz);
+        const RowInfo R = row_info(g, ix, iy, iz);
+        const float* sv = bufs[b] + (int)(((uintptr_t)(V.J + seg[b]) & 15) / sizeof(float));
+        const float q = row_apply_f<1>(g, R, sv + (R.rp - seg[b]), V.p);
+        V.q[n] = q;
+        pq = fmaf(V.p[n], q, pq);
+      }
+      __syncthreads();
+      b ^= 1;
+    }
+  } else {
+    for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
       int ix, iy, iz;
       decompose(g, n, ix, iy, iz);
-      R = row_info(g, ix, iy, iz);
-    }
-    const float* vals = stage_rows<P, float>(g, nrows, V.J, R.rp, smem_raw, tile);
-    if (act) {
-      float q = row_apply_f<P>(g, R, vals, V.p);
+      const RowInfo R = row_info(g, ix, iy, iz);
+      const float q = row_apply_f<P>(g, R, V.J + R.rp, V.p);
       V.q[n] = q;
       pq = fmaf(V.p[n], q, pq);
     }
-    if (P == 1) __syncthreads();
   }
   double m[1] = {block_sum((double)pq)};
   if (last_block<1>(V.parts, m, &V.s->counter)) {
@@ -466,7 +593,27 @@ __global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) 
   if (((volatile PcgScal*)V.s)->done) return;
   const float alpha = (float)V.s->alpha;
   float rr = 0.0f, rz = 0.0f;
-  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
+  const int64_t st = (int64_t)gridDim.x * ST;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  for (; n + 3 * st < nrows; n += 4 * st) {
+    float p[4], q[4], r[4], x[4], mi[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      p[k] = V.p[n + k * st]; q[k] = V.q[n + k * st]; r[k] = V.r[n + k * st];
+      x[k] = V.x[n + k * st]; mi[k] = V.minv[n + k * st];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      V.x[n + k * st] = fmaf(alpha, p[k], x[k]);
+      const float rn = fmaf(-alpha, q[k], r[k]);
+      const float z = rn * mi[k];
+      V.r[n + k * st] = rn;
+      V.z[n + k * st] = z;
+      rr = fmaf(rn, rn, rr);
+      rz = fmaf(rn, z, rz);
+    }
+  }
+  for (; n < nrows; n += st) {
     V.x[n] = fmaf(alpha, V.p[n], V.x[n]);
     float r = fmaf(-alpha, V.q[n], V.r[n]);
     float z = r * V.minv[n];
@@ -495,8 +642,16 @@ __global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) 
 __global__ void __launch_bounds__(ST) k_pcg32_dir(int64_t nrows, PcgVec32 V) {
   if (((volatile PcgScal*)V.s)->done) return;
   const float beta = (float)V.s->beta;
-  for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST)
-    V.p[n] = fmaf(beta, V.p[n], V.z[n]);
+  const int64_t st = (int64_t)gridDim.x * ST;
+  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
+  for (; n + 3 * st < nrows; n += 4 * st) {
+    float p[4], z[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { p[k] = V.p[n + k * st]; z[k] = V.z[n + k * st]; }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) V.p[n + k * st] = fmaf(beta, p[k], z[k]);
+  }
+  for (; n < nrows; n += st) V.p[n] = fmaf(beta, V.p[n], V.z[n]);
 }
 
 // u += (double) du32   (mixed path update; Dirichlet rows have du = 0 because r = 0 there)
@@ -535,7 +690,7 @@ __global__ void __launch_bounds__(ST) k_norminf(int64_t n, const double* __restr
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 // grid of the PCG kernels: one CTA per 128-row tile, at most 8 CTAs per SM
-inline unsigned pcg_grid(const mrg_problem* p) {
+inline unsigned pcg_grid(const mrg_problem* p, int per_sm = 16) {
   static int nsm = 0;
   if (nsm == 0) {
     int dev = 0;
@@ -543,9 +698,16 @@ inline unsigned pcg_grid(const mrg_problem* p) {
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
   }
   const unsigned tiles = nblk(p->ndof, ST);
-  const unsigned cap = (unsigned)(8 * nsm);
+  const unsigned cap = (unsigned)(per_sm * nsm);
   return tiles < cap ? tiles : cap;
 }
+
+// dynamic shared memory of the PCG SpMV: two staging buffers for P = 1
+template <int P, typename JT>
+constexpr int spmv_smem() { return P == 1 ? 2 * stage_elems<JT>() * (int)sizeof(JT) : 0; }
+// CTAs per SM the SpMV grid is sized for (shared-memory bound for P = 1)
+template <int P, typename JT>
+constexpr int spmv_per_sm() { return P == 1 ? (sizeof(JT) == 8 ? 4 : 7) : 16; }
 
 }  // namespace
 
@@ -591,6 +753,12 @@ static int ensure_work(mrg_problem* p, bool need64, bool need32, cudaStream_t st
   }
   SolverWork* w = p->work;
   const int64_t n = p->ndof;
+  static bool attrs = false;  // opt in to more than 48 KB of dynamic shared memory (once per process)
+  if (!attrs) {
+    MRG_CUDA(cudaFuncSetAttribute(k_pcg64_spmv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, spmv_smem<1, double>()));
+    MRG_CUDA(cudaFuncSetAttribute(k_pcg32_spmv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, spmv_smem<1, float>()));
+    attrs = true;
+  }
   const size_t nparts = 3 * (size_t)nblk(n, ST) + 64;
   if (!w->parts) MRG_CUDA(cudaMallocAsync(&w->parts, nparts * sizeof(double), st));
   if (!w->s) {
@@ -619,8 +787,9 @@ static int ensure_work(mrg_problem* p, bool need64, bool need32, cudaStream_t st
 template <int P>
 static void enqueue_chunk64(const mrg_problem* p, const PcgVec64& V, cudaStream_t s) {
   const unsigned nb = pcg_grid(p);
+  const unsigned nbs = pcg_grid(p, spmv_per_sm<P, double>());
   for (int it = 0; it < CHUNK; ++it) {
-    k_pcg64_spmv<P><<<nb, ST, stage_bytes<P, double>(), s>>>(p->g, p->ndof, V);
+    k_pcg64_spmv<P><<<nbs, ST, spmv_smem<P, double>(), s>>>(p->g, p->ndof, V);
     k_pcg64_update<<<nb, ST, 0, s>>>(p->ndof, V);
     k_pcg64_dir<<<nb, ST, 0, s>>>(p->ndof, V);
   }
@@ -628,8 +797,9 @@ static void enqueue_chunk64(const mrg_problem* p, const PcgVec64& V, cudaStream_
 template <int P>
 static void enqueue_chunk32(const mrg_problem* p, const PcgVec32& V, cudaStream_t s) {
   const unsigned nb = pcg_grid(p);
+  const unsigned nbs = pcg_grid(p, spmv_per_sm<P, float>());
   for (int it = 0; it < CHUNK; ++it) {
-    k_pcg32_spmv<P><<<nb, ST, stage_bytes<P, float>(), s>>>(p->g, p->ndof, V);
+    k_pcg32_spmv<P><<<nbs, ST, spmv_smem<P, float>(), s>>>(p->g, p->ndof, V);
     k_pcg32_update<<<nb, ST, 0, s>>>(p->ndof, V);
     k_pcg32_dir<<<nb, ST, 0, s>>>(p->ndof, V);
   }
@@ -957,6 +1127,8 @@ extern "C" int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J, const doub
   NoAllocScratch* S = nullptr;
   int rc = noalloc_scratch(&S);
   if (rc) return rc;
+  // the SpMV stages two CSR tiles in more than 48 KB of dynamic shared memory
+  MRG_CUDA(cudaFuncSetAttribute(k_pcg64_spmv<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, spmv_smem<1, double>()));
   cudaStream_t s = (cudaStream_t)stream;
   PcgVec64 V{x, S->vec[0], S->vec[1], S->vec[2], S->vec[3], S->vec[4], S->parts, b, J, &S->scal};
   k_na_init_scal<<<1, 1, 0, s>>>(&S->scal, rtol, maxiter);

@@ -85,3 +85,35 @@ def test_q2_nonlinear_newton_matches_oracle(cuda, mixed):
     assert res.rel_residual < 1e-10
     err = np.abs(u.cpu().numpy() - uo).max() / np.abs(uo).max()
     assert err < 1e-9, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("i", [0, 2, 3])
+def test_q2_tensor_core_contractions_match_cuda_cores(cuda, i):
+    """tcgen05 3xTF32 Jacobian == FP32 CUDA-core Jacobian (and the oracle) within the FP32 tolerance."""
+    from mrhyde_gb300 import AssemblyManager
+
+    cfg = _cfg(i)
+    O = oracle_problem(cfg)
+    u = np.random.default_rng(70 + i).uniform(0.0, 0.3, O.ndof)
+    ro, Jo = O.assemble(u)
+    G = gpu_problem(cfg)
+    A = AssemblyManager(G)
+    ud = torch.tensor(u, device="cuda")
+    r1, J1 = G.new_vector(), G.new_matrix_values(fp32=True)
+    r2, J2 = G.new_vector(), G.new_matrix_values(fp32=True)
+    A.assembleJacRes(ud, r1, J1, fp32_jacobian=True, overwrite=True)
+    A.assembleJacRes(ud, r2, J2, fp32_jacobian=True, overwrite=True, tensor_cores=True)
+    assert torch.equal(r1, r2)
+    assert scaled_err(J2.cpu().numpy(), J1.cpu().numpy()) <= TOL32_Q2
+    assert scaled_err(J2.cpu().numpy(), Jo) <= TOL32_Q2
+    # sum-into semantics on the tensor-core path
+    J3 = J2.clone()
+    A.assembleJac(ud, J3, fp32_jacobian=True, tensor_cores=True)
+    d, _ = G.fixed_dofs()
+    rp, ci = G.graph()
+    rpn, cin = rp.cpu().numpy(), ci.cpu().numpy()
+    diag = [rpn[k] + np.searchsorted(cin[rpn[k]:rpn[k + 1]], k) for k in d.cpu().numpy()]
+    expect = 2 * J2.cpu().numpy().astype(np.float64)
+    expect[diag] = 1.0
+    np.testing.assert_allclose(J3.cpu().numpy(), expect, rtol=1e-6, atol=0)
