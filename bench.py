@@ -279,7 +279,13 @@ def run_ours(args, rank, world, local_rank):
     ach64 = algo64 / (ms_step * 1e-3) / 1e9
     traffic = read_profile_traffic("k_fact_hex_fp64_c2_128")
     dp_ops = 73 * (info.n_dofs - info.n_fixed)  # FP64 instructions per launch (19 DADD + 27 DMUL + 27 DFMA per free row)
-    dp_peak = 0.507e12  # measured DFMA instructions/s on this GB300 (FP64 pipe), see profiles/fp64_pipe_gb300.md
+    import ctypes
+
+    from mrhyde_gb300 import _lib as LL
+
+    r64, r32 = ctypes.c_double(0), ctypes.c_double(0)
+    LL.check(LL.lib().mrg_measure_fma_rates(ctypes.byref(r64), ctypes.byref(r32), stream.cuda_stream), "fma rates")
+    dp_peak = r64.value  # FP64 FMA instructions/s measured live on this GPU
 
     out = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
@@ -300,7 +306,9 @@ def run_ours(args, rank, world, local_rank):
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": algo64,
                      "fp64_pipe": {"dp_instr_per_launch": dp_ops, "achieved_dp_instr_per_s": dp_ops / (ms_step * 1e-3),
-                                   "peak_dp_instr_per_s": dp_peak, "frac": dp_ops / (ms_step * 1e-3) / dp_peak}},
+                                   "peak_dp_instr_per_s": dp_peak, "frac": dp_ops / (ms_step * 1e-3) / dp_peak,
+                                   "peak_source": "measured in this run (mrg_measure_fma_rates)",
+                                   "fp32_fma_per_s": r32.value}},
         "e2e": {"value": world * cells * n_e2e / (tot_e2e * 1e-3), "unit": "cells/s",
                 "h2d_bytes_per_step": info.n_dofs * 8, "d2h_bytes_per_step": info.nnz * 8 + info.n_dofs * 8},
         "gpu_launches": args.steps,
@@ -383,11 +391,17 @@ def bench_c3(args):
     r = P.new_vector()
     J32 = P.new_matrix_values(fp32=True)
     t_res = _ev_time(lambda: A.assembleRes(u, r, overwrite=True), 5)
-    t_j32 = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True), 3)
+    t_j32 = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True, tensor_cores=False), 3)
+    t_jtc = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True, tensor_cores=True), 3)
+    t_j32_only = _ev_time(lambda: A.assembleJac(u, J32, fp32_jacobian=True, overwrite=True, tensor_cores=False), 3)
+    t_jtc_only = _ev_time(lambda: A.assembleJac(u, J32, fp32_jacobian=True, overwrite=True, tensor_cores=True), 3)
     out = {"workload": f"{args.c3_n}^3 Q2 hex, 27 nodes/cell, 3x3x3 Gauss, u=0 on x=0,1", "cells": info.n_cells,
            "dofs": info.n_dofs, "nnz": info.nnz,
            "residual_fp64_ms": t_res, "residual_cells_per_s": info.n_cells / (t_res * 1e-3),
-           "jac_fp32_plus_res_ms": t_j32, "jac_fp32_cells_per_s": info.n_cells / (t_j32 * 1e-3)}
+           "jac_fp32_plus_res_ms_cuda_cores": t_j32, "jac_fp32_plus_res_ms_tensor_cores": t_jtc,
+           "jac_fp32_cells_per_s_tensor_cores": info.n_cells / (t_jtc * 1e-3),
+           "jac_only_ms_cuda_cores": t_j32_only, "jac_only_ms_tensor_cores": t_jtc_only,
+           "contraction_tflops_tensor_cores": 2.0 * 27 * 27 * 108 * info.n_cells / (t_jtc_only * 1e-3) / 1e12}
     del J32
     torch.cuda.empty_cache()
     S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=25, linear_tol=1e-3, linear_maxiter=20000,
@@ -471,6 +485,19 @@ def run_profile(args, local_rank):
 
     torch.cuda.set_device(local_rank)
     mrhyde_gb300.load()
+    if args.profile in ("q2tc", "q2cc"):
+        from mrhyde_gb300.workloads import c3
+
+        cfg, u0 = c3(seed=3, n=args.c3_n)
+        P = Problem(**cfg)
+        A = AssemblyManager(P)
+        u = torch.tensor(u0, device="cuda")
+        r, J = P.new_vector(), P.new_matrix_values(fp32=True)
+        for _ in range(args.warmup + args.steps):
+            A.assembleJacRes(u, r, J, fp32_jacobian=True, overwrite=True, tensor_cores=(args.profile == "q2tc"))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.profile, "n": args.c3_n, "steps": args.steps, "ok": True}))
+        return
     P = Problem(**c2(seed=2, n=args.n))
     A, S = AssemblyManager(P), SolverManager(P)
     u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, P.info.n_dofs), device="cuda")
@@ -504,7 +531,7 @@ def main():
     ap.add_argument("--c3-n", type=int, default=64)
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32"],
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

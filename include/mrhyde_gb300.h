@@ -120,7 +120,9 @@ enum {
   MRG_ASM_ATOMIC = 512u,       /* per-cell path: atomic scatter instead of 8-colour scatter */
   MRG_ASM_ADJOINT = 1024u,     /* not supported -> MRG_ENOTSUP                   */
   MRG_ASM_SENS = 2048u,        /* not supported -> MRG_ENOTSUP                   */
-  MRG_ASM_TENSOR_CORES = 4096u /* Q2 FP32 Jacobian: element contractions on tcgen05 tensor cores (3xTF32) */
+  MRG_ASM_TENSOR_CORES = 4096u,/* Q2 FP32 Jacobian: element contractions on tcgen05 tensor cores (3xTF32);
+                                  the default for Q2 FP32 Jacobians, kept for explicitness */
+  MRG_ASM_CUDA_CORES = 8192u   /* Q2 FP32 Jacobian: force the CUDA-core contraction instead */
 };
 
 /* ---- problem lifetime ------------------------------------------------------------------------- */
@@ -168,13 +170,24 @@ typedef struct mrg_solve_stats {
 int mrg_solve_pcg(mrg_problem* p, const void* J_vals_dev, int32_t J_fp32, const double* b_dev, double* x_dev,
                   double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
 
+/* Jacobi-preconditioned BiCGStab on J x = b for nonsymmetric Jacobians (x holds the initial guess).
+   The reference offers the same method as "Belos solver: BiCGStab"
+   (src/interfaces/linear_algebra/linearAlgebraInterface_solvers.hpp:108-110).  J_fp32: FP32 matrix,
+   solved for the correction in FP32 vectors.  Synchronises `stream` once at the end. */
+int mrg_solve_bicgstab(mrg_problem* p, const void* J_vals_dev, int32_t J_fp32, const double* b_dev, double* x_dev,
+                       double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
+
+enum { MRG_KRYLOV_AUTO = 0, MRG_KRYLOV_PCG = 1, MRG_KRYLOV_BICGSTAB = 2 };
+
 typedef struct mrg_newton_opts {
   double nl_tol;        /* relative inf-norm tolerance ("nonlinear TOL")                       */
   int32_t max_iters;    /* "max nonlinear iters"                                                */
-  int32_t mixed;        /* 1: FP32 Jacobian + FP32 inner PCG, FP64 residual and update          */
-  double lin_tol;       /* PCG relative tolerance (FP64 path) or inner tolerance (mixed path)   */
+  int32_t mixed;        /* 1: FP32 Jacobian + FP32 inner Krylov, FP64 residual and update       */
+  double lin_tol;       /* Krylov relative tolerance (FP64 path) or inner tolerance (mixed)     */
   int32_t lin_maxiter;
   int32_t reuse_jacobian; /* 1: assemble J once (linear problems)                              */
+  int32_t krylov;       /* MRG_KRYLOV_*: AUTO = PCG for the symmetric thermal form, BiCGStab for 1+u^2 */
+  int32_t reserved;
 } mrg_newton_opts;
 
 /* Newton on F(u) = 0 with u on device (holding the initial guess; Dirichlet values are set first).
@@ -237,6 +250,10 @@ int mrg_batch_set_config(mrg_batch* b, int32_t threads, int32_t ctas_per_sm);
 #define MRG_NOALLOC_MAX_DOFS (1 << 18)
 int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J_vals_dev, const double* b_dev, double* x_dev,
                           double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
+
+/* Sustained FP64 and FP32 FMA issue rates of the current GPU (instructions per second), measured with
+   an FMA-throughput kernel; the denominator of the FP64-pipe roofline.  No counterpart in the reference. */
+int mrg_measure_fma_rates(double* fp64_fma_per_s, double* fp32_fma_per_s, mrg_stream_t stream);
 
 /* ---- diagnostics ----------------------------------------------------------------------------- */
 int mrg_last_error(char* buf, size_t len);   /* copies the calling thread's last error message */

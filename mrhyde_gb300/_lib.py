@@ -31,6 +31,7 @@ MRG_ASM_ATOMIC = 512
 MRG_ASM_ADJOINT = 1024
 MRG_ASM_SENS = 2048
 MRG_ASM_TENSOR_CORES = 4096
+MRG_ASM_CUDA_CORES = 8192
 MRG_NOALLOC_MAX_DOFS = 1 << 18
 
 
@@ -59,9 +60,13 @@ class SolveStats(C.Structure):
                 ("abs_residual", C.c_double), ("status", C.c_int32), ("reserved", C.c_int32)]
 
 
+MRG_KRYLOV_AUTO, MRG_KRYLOV_PCG, MRG_KRYLOV_BICGSTAB = 0, 1, 2
+
+
 class NewtonOpts(C.Structure):
     _fields_ = [("nl_tol", C.c_double), ("max_iters", C.c_int32), ("mixed", C.c_int32),
-                ("lin_tol", C.c_double), ("lin_maxiter", C.c_int32), ("reuse_jacobian", C.c_int32)]
+                ("lin_tol", C.c_double), ("lin_maxiter", C.c_int32), ("reuse_jacobian", C.c_int32),
+                ("krylov", C.c_int32), ("reserved", C.c_int32)]
 
 
 class BatchDesc(C.Structure):
@@ -99,6 +104,7 @@ SIGNATURES = {
     "mrg_spmv": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "mrg_solve_pcg": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_newton": (C.c_int, [_VP, _VP, C.POINTER(NewtonOpts), C.POINTER(SolveStats), _VP]),
+    "mrg_solve_bicgstab": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_solve_pcg_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_batch_create": (C.c_int, [C.POINTER(BatchDesc), C.POINTER(_VP)]),
     "mrg_batch_destroy": (C.c_int, [_VP]),
@@ -106,6 +112,7 @@ SIGNATURES = {
     "mrg_batch_solve": (C.c_int, [_VP, _VP, _VP, C.POINTER(BatchOpts), _VP, _VP]),
     "mrg_batch_autotune": (C.c_int, [_VP, _VP, _VP, C.POINTER(BatchOpts), _VP]),
     "mrg_batch_set_config": (C.c_int, [_VP, C.c_int32, C.c_int32]),
+    "mrg_measure_fma_rates": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
     "mrg_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "mrg_version": (C.c_char_p, []),
 }

@@ -175,7 +175,7 @@ class AssemblyManager:
 
     def assembleJacRes(self, u, res, J, compute_jacobian=True, fp32_jacobian=False, overwrite=False,
                        compute_sens=False, is_adjoint=False, fix_zero_rows=False, force_cell=False, atomic=False,
-                       stream=None, tensor_cores=False):
+                       stream=None, tensor_cores=None):
         """r += -res.val(), J += res.dx(); Dirichlet rows skipped, then J(d,d) = 1.
 
         ``overwrite=True`` fuses the caller's ``J.setAllToScalar(0); r.putScalar(0)``.
@@ -193,8 +193,8 @@ class AssemblyManager:
             flags |= L.MRG_ASM_FORCE_CELL
         if atomic:
             flags |= L.MRG_ASM_ATOMIC
-        if tensor_cores:
-            flags |= L.MRG_ASM_TENSOR_CORES
+        if tensor_cores is not None:  # Q2 FP32 Jacobians use the tensor cores unless told otherwise
+            flags |= L.MRG_ASM_TENSOR_CORES if tensor_cores else L.MRG_ASM_CUDA_CORES
         if compute_sens:
             flags |= L.MRG_ASM_SENS
         if is_adjoint:
@@ -205,9 +205,10 @@ class AssemblyManager:
                                      flags, _stream(stream)), "mrg_assemble")
 
     def assembleJac(self, u, J, fp32_jacobian=False, overwrite=False, force_cell=False, atomic=False, stream=None,
-                    tensor_cores=False):
+                    tensor_cores=None):
         flags = L.MRG_ASM_JAC | (L.MRG_ASM_J_FP32 if fp32_jacobian else 0) | (L.MRG_ASM_OVERWRITE if overwrite else 0)
-        flags |= L.MRG_ASM_TENSOR_CORES if tensor_cores else 0
+        if tensor_cores is not None:
+            flags |= L.MRG_ASM_TENSOR_CORES if tensor_cores else L.MRG_ASM_CUDA_CORES
         flags |= (L.MRG_ASM_FORCE_CELL if force_cell else 0) | (L.MRG_ASM_ATOMIC if atomic else 0)
         self._check_args(u, None, J, False, True, fp32_jacobian)
         L.check(L.lib().mrg_assemble(self.problem.handle, _ptr(u), None, _ptr(J), flags, _stream(stream)),

@@ -510,7 +510,7 @@ int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t 
   int st = (P == 2) ? launch_res_t<2>(p, u, doR ? r : nullptr, qbuf, fp32, mode, s)
                     : launch_res_t<1>(p, u, doR ? r : nullptr, qbuf, fp32, mode, s);
   if (st) return st;
-  if (doJ && P == 2 && fp32 && (flags & MRG_ASM_TENSOR_CORES)) {
+  if (doJ && P == 2 && fp32 && !(flags & MRG_ASM_CUDA_CORES)) {
     MRG_CUDA(cudaMemsetAsync(Q->d_err, 0, sizeof(int), s));
     st = mrg_launch_q2_jac_tc(p, Q->d_tab32, (const float*)qbuf, (float*)J, ovw, Q->d_err, Q->T.s[0], Q->T.s[1],
                               Q->T.s[2], s);

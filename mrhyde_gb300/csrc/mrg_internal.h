@@ -100,6 +100,7 @@ struct mrg_problem {
   std::vector<double> qtab_host;
   std::vector<double> gx1, gw1;  // 1-D Gauss rule of the problem
   void* q2 = nullptr;            // Q2 tensor-product data (mrg_assemble_q2.cu)
+  void* bicg = nullptr;          // BiCGStab workspace (mrg_bicgstab.cu)
   cudaStream_t stream = nullptr;       // creation stream: the handle's memory is allocated/freed in its order
   cudaStream_t last_stream = nullptr;  // last stream work was enqueued on (drained before destroy)
   SolverWork* work = nullptr;
@@ -130,3 +131,10 @@ int mrg_launch_q2_jac_tc(const mrg_problem* p, const float* tab32, const float* 
                          double s0, double s1, double s2, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);
+int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s);  // res = b - res
+// BiCGStab (mrg_bicgstab.cu)
+void mrg_bicg_free(mrg_problem* p);
+int mrg_bicg_solve32(mrg_problem* p, const float* J32, const double* b, double rtol, int maxiter,
+                     mrg_solve_stats* st, const float** d, cudaStream_t s);
+int mrg_bicg_solve64(mrg_problem* p, const double* J, const double* b, double* x, double rtol, int maxiter,
+                     mrg_solve_stats* st, cudaStream_t s);

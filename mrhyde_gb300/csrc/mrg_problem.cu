@@ -173,6 +173,7 @@ static void free_problem(mrg_problem* p) {
   cudaStream_t s = p->stream;
   if (p->last_stream != s) cudaStreamSynchronize(p->last_stream);
   mrg_solver_free(p);
+  mrg_bicg_free(p);
   mrg_q2_free(p);
   cudaFreeAsync(p->d_prefix, s);
   cudaFreeAsync(p->d_kappa, s);

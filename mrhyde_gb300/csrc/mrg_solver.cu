@@ -959,6 +959,17 @@ extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const 
   return MRG_OK;
 }
 
+__global__ void k_b_minus(int64_t n, const double* __restrict__ b, double* __restrict__ res) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) res[i] = b[i] - res[i];
+}
+
+int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s) {
+  k_b_minus<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, b, res);
+  MRG_CUDA(cudaGetLastError());
+  return MRG_OK;
+}
+
 static int norm_inf(mrg_problem* p, const double* v, double* out, cudaStream_t s) {
   SolverWork* w = p->work;
   k_norminf<<<pcg_grid(p), ST, 0, s>>>(p->ndof, v, w->parts, w->s);
@@ -1019,10 +1030,19 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
         have_J = true;
       }
       mrg_solve_stats ls{};
+      // the 1+u^2 Jacobian is nonsymmetric (2 u phi_j grad u . grad phi_i): BiCGStab; CG otherwise
+      const bool bicg = (o->krylov == MRG_KRYLOV_BICGSTAB) || (o->krylov == MRG_KRYLOV_AUTO && p->kind != MRG_THERMAL);
       if (!mixed) {
         MRG_CUDA(cudaMemsetAsync(w->du, 0, p->ndof * sizeof(double), s));
-        rc = pcg64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s);
-        if (rc && rc != MRG_ENOCONV) return rc;
+        rc = bicg ? mrg_bicg_solve64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s)
+                  : pcg64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s);
+        if (rc && rc != MRG_ENOCONV && !(bicg && rc == MRG_ENUMERIC)) return rc;
+      } else if (bicg) {
+        const float* d = nullptr;
+        rc = mrg_bicg_solve32(p, w->J32, w->F, o->lin_tol, o->lin_maxiter, &ls, &d, s);
+        if (rc && rc != MRG_ENOCONV && rc != MRG_ENUMERIC) return rc;
+        k_f32_to_f64<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, d, w->du);
+        MRG_CUDA(cudaGetLastError());
       } else {
         rc = pcg32(p, w->J32, w->F, o->lin_tol, o->lin_maxiter, &ls, s);
         if (rc) return rc;

@@ -8,7 +8,7 @@
 // (l = local index of the row's node in the cell).  A CTA owns 32 consecutive CSR rows, enumerates their
 // (row, cell) pairs in a fixed order, builds A for up to 128 pairs at a time in shared memory, and one
 // thread issues tcgen05.mma (M = 128, N = 32, K = 8 per instruction, 14 K steps) into a 32-column TMEM
-// accumulator.  Each operand is split x = hi + lo with hi = x truncated to TF32, and D accumulates
+// accumulator.  Each operand is split x = hi + lo with hi = x rounded to TF32, and D accumulates
 // A_hi B_hi + A_hi B_lo + A_lo B_hi in FP32 (3xTF32: ~2^-21 relative per product, i.e. FP32-class).
 // The accumulator rows are read back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pairs),
 // parked in shared memory, and each row's pairs are summed in a fixed order into the CTA's staged CSR
@@ -65,7 +65,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 // kind::tf32 instruction descriptor: D = F32, A = B = TF32, both K-major, N = 32, M = 128
 constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) | ((uint32_t)(TCT >> 4) << 24);
 
-__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// round to the nearest TF32 value (10 explicit mantissa bits); the remainder x - hi is exact in FP32
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
 
 __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
   asm volatile(

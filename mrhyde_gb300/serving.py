@@ -57,6 +57,8 @@ class Result:
     status: int
     checksum: float
     u: np.ndarray | None = None
+    t_setup: float = 0.0   # problem creation + coefficients on the device
+    t_solve: float = 0.0   # Newton + Krylov
 
 
 def poisson_stream(rate=200.0, count=400, edge=(16, 96), nonlinear_fraction=0.5, mixed=True, seed=5):
@@ -84,6 +86,7 @@ def estimate_bytes(req: Request) -> int:
 def solve_request(req: Request, stream: torch.cuda.Stream, keep_solution=False):
     """Runs one request to completion on `stream`; returns (Result without timing, u on host or None)."""
     n = req.n
+    t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         gen = torch.Generator(device="cuda")
         gen.manual_seed(req.seed)
@@ -101,7 +104,11 @@ def solve_request(req: Request, stream: torch.cuda.Stream, keep_solution=False):
             S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=30,
                               linear_tol=1e-3 if req.mixed else 1e-11, linear_maxiter=20000,
                               mixed_precision=req.mixed)
+            stream.synchronize()
+            t1 = time.perf_counter()
             res = S.nonlinearSolver(u, stream=stream, raise_on_noconv=False)
+            t2 = time.perf_counter()
+            res.t_setup, res.t_solve = t1 - t0, t2 - t1
             uh = u.to("cpu", non_blocking=False) if keep_solution else None
             checksum = float(u.abs().sum().item())
             stream.synchronize()
@@ -173,7 +180,7 @@ class Server:
             self.results.append(Result(req.rid, req.kind, req.n, dofs, end - req.arrival, start - req.arrival,
                                        end - start, res.outer_iterations if res else 0,
                                        res.iterations if res else 0, res.rel_residual if res else float("nan"),
-                                       status, chk, uh))
+                                       status, chk, uh, getattr(res, "t_setup", 0.0), getattr(res, "t_solve", 0.0)))
 
     def run(self, requests, realtime=True):
         """Feeds `requests` at their arrival times (or all at t=0 if not realtime) and serves them."""
@@ -205,7 +212,16 @@ def summarize(results, wall):
     ok = [r for r in results if r.status == L.MRG_OK]
     lat = np.array([r.latency for r in ok]) * 1e3 if ok else np.array([np.nan])
     dofs = sum(r.dofs for r in ok)
-    return {"requests": len(results), "ok": len(ok), "wall_s": wall,
+    by_kind = {}
+    for kind in ("thermal", "nonlinear"):
+        rk = [r for r in ok if r.kind == kind]
+        if rk:
+            by_kind[kind] = {"count": len(rk), "mean_service_ms": 1e3 * float(np.mean([r.service for r in rk])),
+                             "mean_setup_ms": 1e3 * float(np.mean([r.t_setup for r in rk])),
+                             "mean_solve_ms": 1e3 * float(np.mean([r.t_solve for r in rk])),
+                             "mean_krylov_iters": float(np.mean([r.pcg_iters for r in rk])),
+                             "mean_newton_iters": float(np.mean([r.newton_iters for r in rk]))}
+    return {"requests": len(results), "ok": len(ok), "wall_s": wall, "by_kind": by_kind,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(np.mean(lat)), "dof_per_s": dofs / wall, "req_per_s": len(ok) / wall,
             "max_rel_residual": float(max((r.rel_residual for r in ok), default=float("nan")))}

@@ -32,7 +32,7 @@ def _result(st: L.SolveStats) -> SolveResult:
 
 class SolverManager:
     def __init__(self, problem: Problem, nonlinear_tol=1.0e-6, max_nonlinear_iters=10, linear_tol=1.0e-7,
-                 linear_maxiter=100000, mixed_precision=False, reuse_jacobian=False):
+                 linear_maxiter=100000, mixed_precision=False, reuse_jacobian=False, krylov="auto"):
         self.problem = problem
         self.NLtol = nonlinear_tol
         self.maxNLiter = max_nonlinear_iters
@@ -40,6 +40,7 @@ class SolverManager:
         self.linear_maxiter = linear_maxiter
         self.mixed = mixed_precision
         self.reuse_jacobian = reuse_jacobian
+        self.krylov = {"auto": L.MRG_KRYLOV_AUTO, "pcg": L.MRG_KRYLOV_PCG, "bicgstab": L.MRG_KRYLOV_BICGSTAB}[krylov]
 
     def setDirichlet(self, u: torch.Tensor, stream=None):
         _require_cuda(u, "u", torch.float64, self.problem.info.n_dofs)
@@ -69,6 +70,21 @@ class SolverManager:
             L.check(rc, "mrg_solve_pcg")
         return _result(st)
 
+    def BiCGStab(self, J: torch.Tensor, b: torch.Tensor, x: torch.Tensor, tol: float, maxiter: int, stream=None,
+                 raise_on_noconv=True) -> SolveResult:
+        """Jacobi BiCGStab on J x = b ("Belos solver: BiCGStab"); x holds the initial guess."""
+        info = self.problem.info
+        fp32 = J.dtype == torch.float32
+        _require_cuda(J, "J", None, info.nnz)
+        _require_cuda(b, "b", torch.float64, info.n_dofs)
+        _require_cuda(x, "x", torch.float64, info.n_dofs)
+        st = L.SolveStats()
+        rc = L.lib().mrg_solve_bicgstab(self.problem.handle, _ptr(J), int(fp32), _ptr(b), _ptr(x), float(tol),
+                                        int(maxiter), C.byref(st), _stream(stream))
+        if rc != L.MRG_OK and (raise_on_noconv or rc != L.MRG_ENOCONV):
+            L.check(rc, "mrg_solve_bicgstab")
+        return _result(st)
+
     def nonlinearSolver(self, u: torch.Tensor, stream=None, raise_on_noconv=True) -> SolveResult:
         """Newton on F(u) = 0 with relative inf-norm test; u holds the initial guess."""
         _require_cuda(u, "u", torch.float64, self.problem.info.n_dofs)
@@ -79,6 +95,7 @@ class SolverManager:
         o.lin_tol = self.linear_tol
         o.lin_maxiter = self.linear_maxiter
         o.reuse_jacobian = int(self.reuse_jacobian)
+        o.krylov = self.krylov
         st = L.SolveStats()
         rc = L.lib().mrg_newton(self.problem.handle, _ptr(u), C.byref(o), C.byref(st), _stream(stream))
         if rc != L.MRG_OK and (raise_on_noconv or rc != L.MRG_ENOCONV):
