@@ -15,6 +15,10 @@
  *                         (src/managers/assembly/assemblyManager.hpp:237-259, :330-380;
  *                          body src/managers/assembly/assemblyManager_jacres.hpp:121-630, :669-880)
  *   mrg_set_dirichlet     SolverManager::setDirichlet (src/managers/solver/solverManager_util.hpp:60-140)
+ *   mrg_get_side_points   the "side ip" points at which MrHyDE's FunctionManager evaluates boundary data
+ *   mrg_set_face_bc       "Neumann conditions" / "weak Dirichlet" sides: thermal::boundaryResidual
+ *                         (src/physics/thermal.cpp:170-260) in the boundary workset loop of assembleJacRes
+ *                         (src/managers/assembly/assemblyManager_jacres.hpp:485-603)
  *   mrg_spmv              Tpetra CrsMatrix::apply as used by SolverManager::PCG
  *                         (src/managers/solver/solverManager_solvers.hpp:852, :884)
  *   mrg_solve_pcg         SolverManager::PCG (src/managers/solver/solverManager_solvers.hpp:812-901)
@@ -146,6 +150,22 @@ int mrg_get_fixed_dofs(const mrg_problem* p, int32_t* dofs /*[n_fixed]*/, double
 /* ---- coefficients and Dirichlet data --------------------------------------------------------- */
 int mrg_set_kappa(mrg_problem* p, const double* kappa_dev /*[n_cells]*/, mrg_stream_t stream);
 int mrg_set_dirichlet(const mrg_problem* p, double* u_dev /*[n_dofs]*/, mrg_stream_t stream);
+
+/* ---- boundary terms on box faces (thermal.cpp:170-260) --------------------------------------- *
+ * Faces are numbered 0..2*dim-1 = x-, x+, y-, y+, z-, z+ (bit f of MRG_FACE_*).  Side points of a face are
+ * ordered by face cell (first tangential cell index fastest) and then by point of the cell's side rule
+ * (the problem's 1-D Gauss rule on the tangential axes, first tangential axis fastest).
+ *   MRG_BC_NEUMANN         r_i += int_face g phi_i                        (residual only)
+ *   MRG_BC_WEAK_DIRICHLET  Nitsche terms with penalty 10/h, h = face measure^(1/(dim-1)), form_param 1:
+ *                          res_i += 10/h k (u - g) phi_i - k (grad u . n) phi_i - k (u - g) (grad phi_i . n)
+ *                          (k = kappa_c, or 1 + u^2), in r (as -res) and in J.
+ * Box cells only (no vertex_coords): MRG_ENOTSUP otherwise.  A face with a strong Dirichlet condition
+ * cannot also carry one of these (MRG_EINVAL). */
+enum { MRG_BC_NONE = 0, MRG_BC_NEUMANN = 1, MRG_BC_WEAK_DIRICHLET = 2 };
+/* *npts = number of side points of the face; xyz (host, [npts][3], z = 0 in 2-D) may be NULL. */
+int mrg_get_side_points(const mrg_problem* p, int32_t face, int64_t* npts, double* xyz);
+/* g: host array with one value per side point (NULL = 0).  MRG_BC_NONE removes the face's condition. */
+int mrg_set_face_bc(mrg_problem* p, int32_t face, int32_t kind, const double* g);
 
 /* ---- assembly -------------------------------------------------------------------------------- */
 int mrg_assemble(mrg_problem* p, const double* u_dev, double* r_dev, void* J_vals_dev, uint32_t flags,

@@ -19,6 +19,7 @@ MRG_SRC_CONST, MRG_SRC_SINPROD = 0, 1
 MRG_DBC_CONST, MRG_DBC_NODE = 0, 1
 MRG_FACE_XLO, MRG_FACE_XHI, MRG_FACE_YLO, MRG_FACE_YHI, MRG_FACE_ZLO, MRG_FACE_ZHI = 1, 2, 4, 8, 16, 32
 MRG_FACE_ALL = 63
+MRG_BC_NONE, MRG_BC_NEUMANN, MRG_BC_WEAK_DIRICHLET = 0, 1, 2
 MRG_PATH_FACTORED, MRG_PATH_CELL, MRG_PATH_TENSOR = 1, 2, 3
 
 MRG_ASM_RES = 1
@@ -100,6 +101,8 @@ SIGNATURES = {
     "mrg_get_fixed_dofs": (C.c_int, [_VP, _VP, _VP, _VP]),
     "mrg_set_kappa": (C.c_int, [_VP, _VP, _VP]),
     "mrg_set_dirichlet": (C.c_int, [_VP, _VP, _VP]),
+    "mrg_get_side_points": (C.c_int, [_VP, C.c_int32, C.POINTER(C.c_int64), _VP]),
+    "mrg_set_face_bc": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP]),
     "mrg_assemble": (C.c_int, [_VP, _VP, _VP, _VP, C.c_uint32, _VP]),
     "mrg_spmv": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "mrg_solve_pcg": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),

@@ -152,6 +152,24 @@ class Problem:
         _require_cuda(kappa, "kappa", torch.float64, self.info.n_cells)
         L.check(L.lib().mrg_set_kappa(self._h, _ptr(kappa), _stream(stream)), "mrg_set_kappa")
 
+    def side_points(self, face: int) -> np.ndarray:
+        """Coordinates [npts, 3] of the side quadrature points of `face` (0..2*dim-1 = x-, x+, y-, y+,
+        z-, z+), ordered as mrg_set_face_bc expects its data."""
+        n = C.c_int64(0)
+        L.check(L.lib().mrg_get_side_points(self._h, int(face), C.byref(n), None), "mrg_get_side_points")
+        xyz = np.zeros((n.value, 3))
+        L.check(L.lib().mrg_get_side_points(self._h, int(face), C.byref(n), xyz.ctypes.data_as(C.c_void_p)),
+                "mrg_get_side_points")
+        return xyz
+
+    def set_face_bc(self, face: int, kind: str, g=None):
+        """Neumann ("neumann") or weakly imposed Dirichlet ("weak_dirichlet") data on a face, one value per
+        side point (None = 0); "none" removes it.  Reference: thermal::boundaryResidual."""
+        k = {"none": L.MRG_BC_NONE, "neumann": L.MRG_BC_NEUMANN, "weak_dirichlet": L.MRG_BC_WEAK_DIRICHLET}[kind]
+        ga = None if g is None else np.ascontiguousarray(g, dtype=np.float64)
+        L.check(L.lib().mrg_set_face_bc(self._h, int(face), k, None if ga is None else ga.ctypes.data_as(C.c_void_p)),
+                "mrg_set_face_bc")
+
     def new_vector(self, dtype=torch.float64):
         return torch.zeros(self.info.n_dofs, dtype=dtype, device="cuda")
 

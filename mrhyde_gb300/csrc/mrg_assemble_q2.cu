@@ -54,12 +54,19 @@ __device__ __forceinline__ void split3(int l, int n1, int& i0, int& i1, int& i2)
 
 constexpr int RW = 8;  // warps per CTA in the residual kernel
 
+// round to the nearest TF32 value (10 explicit mantissa bits, ties away from zero)
+__device__ __forceinline__ float tf32_rn(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
 // mode bits: 1 = scatter residual, 2 = store qp coefficients (QT precision)
 template <int P, typename QT>
 __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int color, int cc0, int cc1, int64_t ncl,
                                                     int kind, const double* __restrict__ u,
                                                     const double* __restrict__ kap, double* __restrict__ r,
-                                                    QT* __restrict__ qbuf, int mode) {
+                                                    QT* __restrict__ qbuf, int tc_image, int mode) {
   using K = TP<P>;
   constexpr int N1 = K::N1, NL = K::NL;
   __shared__ double sm[RW][K::CPW][6][NL];
@@ -149,12 +156,27 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
     Fz = cw * T.s[2] * T.s[2] * gz;
     if (mode & 2) {
       QT* qb = qbuf + cid * K::NQB;
-      qb[l] = (QT)cw;
+      // tc_image (FP32 only): split x = hi + lo (hi = x rounded to TF32, lo = the remainder rounded to
+      // TF32) and store both into the tensor-core operand image [tile][hi, lo][K chunk][cell][4] with
+      // 128-cell tiles and 112 K slots; otherwise plain QT values [cell][4 NL]
+      auto put = [&](int k, double v) {
+        if constexpr (sizeof(QT) == 4) {
+          if (tc_image) {
+            const float hi = tf32_rn((float)v);
+            float* t = qbuf + (cid >> 7) * (2 * 128 * 112) + (k >> 2) * 512 + (cid & 127) * 4 + (k & 3);
+            t[0] = hi;
+            t[128 * 112] = tf32_rn((float)(v - (double)hi));
+            return;
+          }
+        }
+        qb[k] = (QT)v;
+      };
+      put(l, cw);
       if (kind != MRG_THERMAL) {
         const double e = Wq * 2.0 * uq;
-        qb[NL + l] = (QT)(e * T.s[0] * T.s[0] * gx);
-        qb[2 * NL + l] = (QT)(e * T.s[1] * T.s[1] * gy);
-        qb[3 * NL + l] = (QT)(e * T.s[2] * T.s[2] * gz);
+        put(NL + l, e * T.s[0] * T.s[0] * gx);
+        put(2 * NL + l, e * T.s[1] * T.s[1] * gy);
+        put(3 * NL + l, e * T.s[2] * T.s[2] * gz);
       }
     }
   }
@@ -363,6 +385,8 @@ struct TPData {
   void* d_qbuf = nullptr;  // ncell * 4 NL (FP64 or FP32, by the last Jacobian request)
   size_t qbuf_bytes = 0;
   int* d_err = nullptr;    // tensor-core kernel status (bounded waits)
+  std::vector<double> tab_host;  // [G_x | G_y | G_z | Phi] rows of TS doubles
+  Q2Tc* tc = nullptr;      // tensor-core element-matrix plan (Q2, FP32 Jacobian), built on first use
 };
 
 static TPData* tpdata(mrg_problem* p) { return reinterpret_cast<TPData*>(p->q2); }
@@ -419,6 +443,7 @@ int mrg_q2_setup(mrg_problem* p) {
       for (int j = 0; j < NL; ++j)
         tab[(d * NL + q) * TS + j] = (d < 3) ? tdphi[(j * nq + q) * 3 + d] : tphi[j * nq + q];
   for (size_t k = 0; k < tab.size(); ++k) tab32[k] = (float)tab[k];
+  Q->tab_host = tab;
   cudaStream_t s = p->stream;
   MRG_CUDA(cudaMallocAsync(&Q->d_err, sizeof(int), s));
   MRG_CUDA(cudaMemsetAsync(Q->d_err, 0, sizeof(int), s));
@@ -437,22 +462,24 @@ void mrg_q2_free(mrg_problem* p) {
   cudaFreeAsync(Q->d_tab32, p->stream);
   cudaFreeAsync(Q->d_err, p->stream);
   if (Q->d_qbuf) cudaFreeAsync(Q->d_qbuf, p->stream);
+  mrg_q2tc_free(Q->tc, p->stream);
   delete Q;
   p->q2 = nullptr;
 }
 
 template <int P>
-static int launch_res_t(mrg_problem* p, const double* u, double* r, void* qbuf, bool fp32q, int mode, cudaStream_t s) {
+static int launch_res_t(mrg_problem* p, const double* u, double* r, void* qbuf, bool tc_image, bool fp32q, int mode,
+                        cudaStream_t s) {
   TPData* Q = tpdata(p);
   const Grid& g = p->g;
   constexpr int CPB = RW * TP<P>::CPW;  // cells per CTA
   auto launch = [&](int color, int cc0, int cc1, int64_t tot) {
     if (fp32q)
       k_tp_res<P, float><<<nblk(tot, CPB), RW * 32, 0, s>>>(Q->T, g, color, cc0, cc1, tot, p->kind, u, p->d_kappa, r,
-                                                             (float*)qbuf, mode);
+                                                             (float*)qbuf, tc_image ? 1 : 0, mode);
     else
       k_tp_res<P, double><<<nblk(tot, CPB), RW * 32, 0, s>>>(Q->T, g, color, cc0, cc1, tot, p->kind, u, p->d_kappa, r,
-                                                              (double*)qbuf, mode);
+                                                              (double*)qbuf, 0, mode);
     return cudaGetLastError();
   };
   if (mode & 1) {
@@ -494,6 +521,25 @@ int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t 
   const bool doJ = flags & MRG_ASM_JAC, doR = flags & MRG_ASM_RES, ovw = flags & MRG_ASM_OVERWRITE;
   const bool fp32 = flags & MRG_ASM_J_FP32;
   void* qbuf = nullptr;
+  const bool tc = doJ && P == 2 && fp32 && !(flags & MRG_ASM_CUDA_CORES);
+  if (tc) {
+    // tensor cores: the residual pass writes the TF32 hi/lo planes of W straight into the plan's buffer
+    if (!Q->tc) {
+      int st = mrg_q2tc_create(p, Q->tab_host.data(), Q->T.s, &Q->tc, s);
+      if (st) return st;
+    }
+    if (doR && ovw) MRG_CUDA(cudaMemsetAsync(r, 0, p->ndof * sizeof(double), s));
+    int st = launch_res_t<2>(p, u, doR ? r : nullptr, mrg_q2tc_w_image(Q->tc), true, true, (doR ? 1 : 0) | 2, s);
+    if (st) return st;
+    MRG_CUDA(cudaMemsetAsync(Q->d_err, 0, sizeof(int), s));
+    st = mrg_q2tc_launch(p, Q->tc, (float*)J, ovw, Q->d_err, s);
+    if (st) return st;
+    int herr = 0;
+    MRG_CUDA(cudaMemcpyAsync(&herr, Q->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MRG_CUDA(cudaStreamSynchronize(s));
+    if (herr) return mrg_fail(MRG_ETIMEOUT, "tensor-core element kernel: an mbarrier wait timed out");
+    return MRG_OK;
+  }
   if (doJ) {
     const size_t need = (size_t)p->ncell * 4 * NL * (fp32 ? sizeof(float) : sizeof(double));
     if (Q->qbuf_bytes < need) {
@@ -507,20 +553,9 @@ int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t 
   }
   if (doR && ovw) MRG_CUDA(cudaMemsetAsync(r, 0, p->ndof * sizeof(double), s));
   const int mode = (doR ? 1 : 0) | (doJ ? 2 : 0);
-  int st = (P == 2) ? launch_res_t<2>(p, u, doR ? r : nullptr, qbuf, fp32, mode, s)
-                    : launch_res_t<1>(p, u, doR ? r : nullptr, qbuf, fp32, mode, s);
+  int st = (P == 2) ? launch_res_t<2>(p, u, doR ? r : nullptr, qbuf, false, fp32, mode, s)
+                    : launch_res_t<1>(p, u, doR ? r : nullptr, qbuf, false, fp32, mode, s);
   if (st) return st;
-  if (doJ && P == 2 && fp32 && !(flags & MRG_ASM_CUDA_CORES)) {
-    MRG_CUDA(cudaMemsetAsync(Q->d_err, 0, sizeof(int), s));
-    st = mrg_launch_q2_jac_tc(p, Q->d_tab32, (const float*)qbuf, (float*)J, ovw, Q->d_err, Q->T.s[0], Q->T.s[1],
-                              Q->T.s[2], s);
-    if (st) return st;
-    int herr = 0;
-    MRG_CUDA(cudaMemcpyAsync(&herr, Q->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MRG_CUDA(cudaStreamSynchronize(s));
-    if (herr) return mrg_fail(MRG_ETIMEOUT, "tensor-core Jacobian: MMA completion wait timed out");
-    return MRG_OK;
-  }
   if (doJ) {
     cudaError_t e;
     if (P == 2)

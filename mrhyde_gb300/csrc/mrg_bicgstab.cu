@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(BT) k_b_init(Grid g, int64_t nrows, BVec<VT, J
   GSTRIDE(n) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
-    const RowInfo R = row_info(g, ix, iy, iz);
+    const RowInfo R = row_info<P>(g, ix, iy, iz);
     const VT d = (VT)V.J[diag_pos(R, ix, iy, iz)];
     const VT ax = x0_zero ? VT(0) : row_dot<P, JT, VT, VT>(g, R, V.J + R.rp, V.x);
     if (x0_zero) V.x[n] = VT(0);
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(BT) k_b_spmv(Grid g, int64_t nrows, BVec<VT, J
   GSTRIDE(n) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
-    const RowInfo R = row_info(g, ix, iy, iz);
+    const RowInfo R = row_info<P>(g, ix, iy, iz);
     const VT y = row_dot<P, JT, VT, VT>(g, R, V.J + R.rp, in);
     out[n] = y;
     if (STEP == 0) {

@@ -20,11 +20,14 @@ struct RowInfo {
   int64_t rp;
 };
 
+// PC > 0: the polynomial order is a compile-time constant (the axis divisions fold away)
+template <int PC = 0>
 __device__ __forceinline__ RowInfo row_info(const Grid& g, int ix, int iy, int iz) {
   RowInfo R;
-  axis_range(ix, g.nn[0], g.p, R.lx, R.cx);
-  axis_range(iy, g.nn[1], g.p, R.ly, R.cy);
-  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
+  const int p = PC > 0 ? PC : g.p;
+  axis_range(ix, g.nn[0], p, R.lx, R.cx);
+  axis_range(iy, g.nn[1], p, R.ly, R.cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
   R.rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)R.cz * (g.P[1][iy] * g.T[0] + (int64_t)R.cy * g.P[0][ix]);
   return R;
 }

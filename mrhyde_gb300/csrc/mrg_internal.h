@@ -101,6 +101,7 @@ struct mrg_problem {
   std::vector<double> gx1, gw1;  // 1-D Gauss rule of the problem
   void* q2 = nullptr;            // Q2 tensor-product data (mrg_assemble_q2.cu)
   void* bicg = nullptr;          // BiCGStab workspace (mrg_bicgstab.cu)
+  void* bnd = nullptr;           // face boundary conditions (mrg_boundary.cu)
   cudaStream_t stream = nullptr;       // creation stream: the handle's memory is allocated/freed in its order
   cudaStream_t last_stream = nullptr;  // last stream work was enqueued on (drained before destroy)
   SolverWork* work = nullptr;
@@ -126,9 +127,18 @@ int mrg_launch_kappa32(mrg_problem* p, cudaStream_t s);
 int mrg_q2_setup(mrg_problem* p);
 void mrg_q2_free(mrg_problem* p);
 int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s);
-// Q2 Jacobian contractions on tcgen05 tensor cores (mrg_tc_q2.cu)
-int mrg_launch_q2_jac_tc(const mrg_problem* p, const float* tab32, const float* qbuf, float* J, bool ovw, int* err,
-                         double s0, double s1, double s2, cudaStream_t s);
+// Q2 element matrices on tcgen05 tensor cores and their row gather (mrg_tc_q2.cu)
+struct Q2Tc;
+int mrg_q2tc_create(mrg_problem* p, const double* tab, const double s[3], Q2Tc** out, cudaStream_t st);
+void mrg_q2tc_free(Q2Tc* T, cudaStream_t st);
+float* mrg_q2tc_w_image(Q2Tc* T);  // [tile][hi, lo][K chunk 28][cell 128][4] TF32 operand image
+int mrg_q2tc_launch(const mrg_problem* p, Q2Tc* T, float* J, bool ovw, int* err, cudaStream_t s);
+// Face boundary terms (mrg_boundary.cu)
+void mrg_boundary_free(mrg_problem* p);
+bool mrg_boundary_active(const mrg_problem* p);
+int mrg_launch_boundary(mrg_problem* p, const double* u, double* r, void* J, bool fp32, cudaStream_t s);
+// 1-D Lagrange basis of degree p on equispaced nodes of [-1,1]: values l[0..p], derivatives dl[0..p]
+void mrg_lagrange_1d(int p, double xi, double* l, double* dl);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);
 int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s);  // res = b - res

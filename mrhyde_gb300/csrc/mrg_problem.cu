@@ -91,6 +91,8 @@ static void lagrange(int p, double xi, double* l, double* dl) {
   }
 }
 
+void mrg_lagrange_1d(int p, double xi, double* l, double* dl) { lagrange(p, xi, l, dl); }
+
 // ------------------------------------------------------------------------------------------------
 // small kernels
 // ------------------------------------------------------------------------------------------------
@@ -175,6 +177,7 @@ static void free_problem(mrg_problem* p) {
   mrg_solver_free(p);
   mrg_bicg_free(p);
   mrg_q2_free(p);
+  mrg_boundary_free(p);
   cudaFreeAsync(p->d_prefix, s);
   cudaFreeAsync(p->d_kappa, s);
   cudaFreeAsync(p->d_kappa32, s);
@@ -544,6 +547,11 @@ extern "C" int mrg_assemble(mrg_problem* p, const double* u, double* r, void* J,
       st = mrg_launch_constraints(p, J, fp32, s);
       if (st != MRG_OK) return st;
     }
+  }
+  // boundary workset loop (jacres:485-603): Neumann / weak-Dirichlet faces, after the volume terms
+  if (mrg_boundary_active(p)) {
+    st = mrg_launch_boundary(p, u, doR ? r : nullptr, doJ ? J : nullptr, fp32, s);
+    if (st != MRG_OK) return st;
   }
   if (doJ && (flags & MRG_ASM_FIX_ZERO_ROWS)) return mrg_launch_fix_zero_rows(p, J, fp32, s);
   return MRG_OK;

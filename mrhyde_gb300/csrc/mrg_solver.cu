@@ -6,8 +6,11 @@
 //   mrg_newton     SolverManager::nonlinearSolver (src/managers/solver/solverManager_solvers.hpp:290-643)
 //
 // Design: the column indices of the canonical graph are implied by the structured layout, so the
-// SpMV reads only the values (8 or 4 bytes per nonzero) and the source vector.  Every PCG iteration
-// is three kernels (SpMV+dot, vector update+dots, direction update); each dot product is reduced
+// SpMV reads only the values (8 or 4 bytes per nonzero) and the source vector.  For Q1 rows a warp
+// stages the CSR values of its 32 rows in shared memory with one bulk copy (cp.async.bulk on a
+// per-warp mbarrier), double-buffered, with no CTA-wide barrier.  An FP64 PCG iteration is three
+// kernels (SpMV+dot, vector update+dots, direction update); the FP32 inner PCG keeps q = J p by
+// recurrence and folds the direction update into its SpMV (two kernels).  Each dot product is reduced
 // deterministically by the "last block finishes the sum" pattern (partials written per block, a
 // counter incremented after a fence, the last block sums the partials in index order) -- no extra
 // launch, no spinning, and bit-identical results from run to run and independent of what else runs
@@ -74,11 +77,14 @@ struct RowInfo {
   int64_t rp;
 };
 
+// PC > 0: the polynomial order is a compile-time constant (the axis divisions fold away)
+template <int PC = 0>
 __device__ __forceinline__ RowInfo row_info(const Grid& g, int ix, int iy, int iz) {
   RowInfo R;
-  axis_range(ix, g.nn[0], g.p, R.lx, R.cx);
-  axis_range(iy, g.nn[1], g.p, R.ly, R.cy);
-  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
+  const int p = PC > 0 ? PC : g.p;
+  axis_range(ix, g.nn[0], p, R.lx, R.cx);
+  axis_range(iy, g.nn[1], p, R.ly, R.cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
   R.rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)R.cz * (g.P[1][iy] * g.T[0] + (int64_t)R.cy * g.P[0][ix]);
   return R;
 }
@@ -149,6 +155,140 @@ __device__ __forceinline__ int64_t tile_issue(const Grid& g, int64_t nrows, cons
   for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) dst[k] = __ldcs(src + k);
   cp_async_commit();
   return seg0;
+}
+
+// ---- per-warp staged rows (P = 1) --------------------------------------------------------------
+// A warp owns tiles of 32 consecutive rows.  Their CSR values form one contiguous segment, which lane 0
+// copies into the warp's own shared buffer with a 1-D bulk copy (cp.async.bulk, completion counted on
+// the warp's mbarrier) while the warp multiplies its previous tile; the unaligned ends of the segment
+// are copied with plain loads.  No CTA-wide barrier is involved, so warps never wait for each other.
+constexpr int WROWS = 32;
+template <typename JT>
+__host__ __device__ constexpr int wbuf_elems() { return WROWS * 27 + 2 * (16 / (int)sizeof(JT)); }
+template <typename JT>
+constexpr int wspmv_smem() { return (ST / 32) * 2 * wbuf_elems<JT>() * (int)sizeof(JT); }
+
+constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on one tile's copy
+
+__device__ __forceinline__ bool wbar_try(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t wtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+
+// bounded wait by every lane of the warp; the result is warp-uniform
+__device__ __forceinline__ bool wbar_wait(uint32_t mbar, uint32_t parity) {
+  int ok = 1;
+  if (!wbar_try(mbar, parity)) {
+    const uint64_t t0 = wtimer();
+    while (!wbar_try(mbar, parity))
+      if (wtimer() - t0 > WAIT_NS) { ok = 0; break; }
+  }
+  return __all_sync(0xffffffffu, ok) != 0;
+}
+
+// Issues the copy of warp tile `tile` into buf; returns the global byte address mapped to buf[0].
+template <typename JT>
+__device__ __forceinline__ uintptr_t wtile_issue(const Grid& g, int64_t nrows, const JT* __restrict__ J, int64_t tile,
+                                                 JT* buf, uint32_t mbar, int lane) {
+  const int64_t n0 = tile * WROWS;
+  const int64_t n1 = (n0 + WROWS < nrows) ? n0 + WROWS : nrows;
+  const int64_t nnz = g.T[0] * g.T[1] * g.T[2];
+  const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
+  const uintptr_t lo = (uintptr_t)(J + seg0), hi = (uintptr_t)(J + seg1);
+  const uintptr_t base = lo & ~(uintptr_t)15;
+  const uintptr_t jb = ((uintptr_t)J + 15) & ~(uintptr_t)15, je = (uintptr_t)(J + nnz) & ~(uintptr_t)15;
+  uintptr_t b0 = base < jb ? jb : base;
+  uintptr_t b1 = (hi + 15) & ~(uintptr_t)15;
+  if (b1 > je) b1 = je;
+  if (b0 > hi) b0 = hi;
+  if (b1 < b0) b1 = b0;
+  unsigned char* sb = reinterpret_cast<unsigned char*>(buf);
+  // plain loads: head [lo, b0) and tail [max(b1, lo), hi) -- a few elements at most
+  constexpr int E = (int)sizeof(JT);
+  const int nhead = (int)((b0 - lo) / E);
+  const uintptr_t t0 = b1 > lo ? b1 : lo;
+  const int ntail = (int)((hi - t0) / E);
+  if (lane < nhead) *reinterpret_cast<JT*>(sb + (lo - base) + lane * E) = __ldcs(reinterpret_cast<const JT*>(lo) + lane);
+  if (lane >= 8 && lane - 8 < ntail)
+    *reinterpret_cast<JT*>(sb + (t0 - base) + (lane - 8) * E) = __ldcs(reinterpret_cast<const JT*>(t0) + (lane - 8));
+  if (lane == 0) {
+    const uint32_t bytes = (uint32_t)(b1 - b0);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+    if (bytes)
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+              (uint32_t)__cvta_generic_to_shared(sb + (b0 - base))),
+          "l"(b0), "r"(bytes), "r"(mbar)
+          : "memory");
+  }
+  return base;
+}
+
+// Runs f(n, R, vals) for every row n (vals = the row's values in shared memory), warp-tiled and
+// double-buffered.  Returns false if a copy did not complete within the time bound.
+template <typename JT, typename F>
+__device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, const JT* __restrict__ J,
+                                                 unsigned char* smem_raw, uint64_t* mbar_base, F&& f) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  JT* const buf0 = reinterpret_cast<JT*>(smem_raw) + (2 * w) * wbuf_elems<JT>();
+  JT* const buf1 = buf0 + wbuf_elems<JT>();
+  const uint32_t mb0 = (uint32_t)__cvta_generic_to_shared(mbar_base + 2 * w), mb1 = mb0 + 8u;
+  if (lane == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncwarp();
+  const int64_t ntiles = (nrows + WROWS - 1) / WROWS;
+  const int64_t W = (int64_t)gridDim.x * (ST / 32);
+  int64_t tile = (int64_t)blockIdx.x * (ST / 32) + w;
+  // buffer b of the current tile; the other buffer receives the next tile
+  uintptr_t base0 = 0, base1 = 0;
+  uint32_t ph0 = 0u, ph1 = 0u;
+  bool armed0 = false, armed1 = false, ok = true;
+  int b = 0;
+  if (tile < ntiles) {
+    base0 = wtile_issue<JT>(g, nrows, J, tile, buf0, mb0, lane);
+    armed0 = true;
+  }
+  for (; tile < ntiles; tile += W) {
+    const int64_t nxt = tile + W;
+    if (nxt < ntiles) {
+      if (b == 0) { base1 = wtile_issue<JT>(g, nrows, J, nxt, buf1, mb1, lane); armed1 = true; }
+      else        { base0 = wtile_issue<JT>(g, nrows, J, nxt, buf0, mb0, lane); armed0 = true; }
+    }
+    const bool got = (b == 0) ? wbar_wait(mb0, ph0) : wbar_wait(mb1, ph1);
+    if (!got) { ok = false; break; }
+    if (b == 0) { ph0 ^= 1u; armed0 = false; } else { ph1 ^= 1u; armed1 = false; }
+    __syncwarp();
+    const int64_t n = tile * WROWS + lane;
+    if (n < nrows) {
+      int ix, iy, iz;
+      decompose(g, n, ix, iy, iz);
+      const RowInfo R = row_info<1>(g, ix, iy, iz);
+      const unsigned char* cb = reinterpret_cast<const unsigned char*>(b == 0 ? buf0 : buf1);
+      const JT* vals = reinterpret_cast<const JT*>(cb + ((uintptr_t)(J + R.rp) - (b == 0 ? base0 : base1)));
+      f(n, R, vals);
+    }
+    __syncwarp();
+    b ^= 1;
+  }
+  if (!ok) {  // let copies still in flight land before the CTA exits (bounded)
+    if (armed0) wbar_wait(mb0, ph0);
+    if (armed1) wbar_wait(mb1, ph1);
+  }
+  return ok;
 }
 
 // sum of v over the block, returned in thread 0 (FP64)
@@ -309,7 +449,7 @@ __global__ void __launch_bounds__(ST) k_spmv(Grid g, int64_t nrows, const JT* __
   if (act) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
-    R = row_info(g, ix, iy, iz);
+    R = row_info<P>(g, ix, iy, iz);
   }
   const JT* vals = stage_rows<P, JT>(g, nrows, J, R.rp, smem_raw, blockIdx.x);
   if (act) y[n] = row_apply<P, JT, double>(g, R, vals, x);
@@ -332,7 +472,7 @@ __global__ void __launch_bounds__(ST) k_pcg64_init(Grid g, int64_t nrows, PcgVec
   for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
-    RowInfo R = row_info(g, ix, iy, iz);
+    RowInfo R = row_info<P>(g, ix, iy, iz);
     double ax = row_apply<P, double, double>(g, R, V.J + R.rp, V.x);
     double d = V.J[R.rp + ((int64_t)(iz - R.lz) * R.cy + (iy - R.ly)) * R.cx + (ix - R.lx)];
     double mi = 1.0 / d;
@@ -366,42 +506,22 @@ __global__ void __launch_bounds__(ST) k_pcg64_init(Grid g, int64_t nrows, PcgVec
 template <int P>
 __global__ void __launch_bounds__(ST) k_pcg64_spmv(Grid g, int64_t nrows, PcgVec64 V) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2 * (ST / 32)];
   if (((volatile PcgScal*)V.s)->done) return;
   double pq = 0.0;
-  const int64_t ntiles = (nrows + ST - 1) / ST;
   if constexpr (P == 1) {
-    double* bufs[2] = {reinterpret_cast<double*>(smem_raw), reinterpret_cast<double*>(smem_raw) + stage_elems<double>()};
-    int64_t seg[2] = {0, 0};
-    int b = 0;
-    int64_t tile = blockIdx.x;
-    if (tile < ntiles) seg[0] = tile_issue<double>(g, nrows, V.J, tile, bufs[0]);
-    for (; tile < ntiles; tile += gridDim.x) {
-      const int64_t nxt = tile + gridDim.x;
-      if (nxt < ntiles) {
-        seg[b ^ 1] = tile_issue<double>(g, nrows, V.J, nxt, bufs[b ^ 1]);
-        cp_async_wait<1>();
-      } else {
-        cp_async_wait<0>();
-      }
-      __syncthreads();
-      const int64_t n = tile * ST + threadIdx.x;
-      if (n < nrows) {
-        int ix, iy, iz;
-        decompose(g, n, ix, iy, iz);
-        const RowInfo R = row_info(g, ix, iy, iz);
-        const double* sv = bufs[b] + (int)(((uintptr_t)(V.J + seg[b]) & 15) / sizeof(double));
-        const double q = row_apply<1, double, double>(g, R, sv + (R.rp - seg[b]), V.p);
-        V.q[n] = q;
-        pq = fma(V.p[n], q, pq);
-      }
-      __syncthreads();
-      b ^= 1;
-    }
+    const bool ok = warp_staged_rows<double>(g, nrows, V.J, smem_raw, mbar, [&](int64_t n, const RowInfo& R,
+                                                                                  const double* vals) {
+      const double q = row_apply<1, double, double>(g, R, vals, V.p);
+      V.q[n] = q;
+      pq = fma(V.p[n], q, pq);
+    });
+    if (!ok) { V.s->status = MRG_ETIMEOUT; V.s->done = 1; }
   } else {
     for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
       int ix, iy, iz;
       decompose(g, n, ix, iy, iz);
-      const RowInfo R = row_info(g, ix, iy, iz);
+      const RowInfo R = row_info<P>(g, ix, iy, iz);
       const double q = row_apply<P, double, double>(g, R, V.J + R.rp, V.p);
       V.q[n] = q;
       pq = fma(V.p[n], q, pq);
@@ -502,7 +622,7 @@ __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec
   for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
-    RowInfo R = row_info(g, ix, iy, iz);
+    RowInfo R = row_info<P>(g, ix, iy, iz);
     float d = V.J[R.rp + ((int64_t)(iz - R.lz) * R.cy + (iy - R.ly)) * R.cx + (ix - R.lx)];
     float mi = 1.0f / d;
     float r = (float)V.b[n];   // x0 = 0
@@ -512,6 +632,7 @@ __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec
     V.r[n] = r;
     V.z[n] = z;
     V.p[n] = z;
+    V.q[n] = 0.0f;
     rr += (double)(r * r);
     rz += (double)(r * z);
   }
@@ -521,6 +642,7 @@ __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec
     sum_parts<2>(V.parts, t, &V.s->counter);
     if (threadIdx.x == 0) {
       PcgScal* s = V.s;
+      s->beta = 0.0;
       s->r0 = sqrt(t[0]);
       s->rnorm = s->r0;
       s->rho = t[1];
@@ -532,48 +654,37 @@ __global__ void __launch_bounds__(ST) k_pcg32_init(Grid g, int64_t nrows, PcgVec
   }
 }
 
+// FP32 PCG, direction and product in one pass.  With q = J p maintained by recurrence,
+//   p <- z + beta p,   q <- J z + beta q   (= J p by linearity),
+// so the SpMV reads z and the separate direction update of the classic loop disappears: one
+// iteration is this kernel plus k_pcg32_update.  Partial p.q; last block: alpha = rho / (p.q).
+// Before the first iteration p = z, q = 0 and beta = 0.
 template <int P>
 __global__ void __launch_bounds__(ST) k_pcg32_spmv(Grid g, int64_t nrows, PcgVec32 V) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2 * (ST / 32)];
   if (((volatile PcgScal*)V.s)->done) return;
+  const float beta = (float)V.s->beta;
   float pq = 0.0f;
-  const int64_t ntiles = (nrows + ST - 1) / ST;
+  auto fin = [&](int64_t n, float w) {
+    const float pn = fmaf(beta, V.p[n], V.z[n]);
+    const float qn = fmaf(beta, V.q[n], w);
+    V.p[n] = pn;
+    V.q[n] = qn;
+    pq = fmaf(pn, qn, pq);
+  };
   if constexpr (P == 1) {
-    float* bufs[2] = {reinterpret_cast<float*>(smem_raw), reinterpret_cast<float*>(smem_raw) + stage_elems<float>()};
-    int64_t seg[2] = {0, 0};
-    int b = 0;
-    int64_t tile = blockIdx.x;
-    if (tile < ntiles) seg[0] = tile_issue<float>(g, nrows, V.J, tile, bufs[0]);
-    for (; tile < ntiles; tile += gridDim.x) {
-      const int64_t nxt = tile + gridDim.x;
-      if (nxt < ntiles) {
-        seg[b ^ 1] = tile_issue<float>(g, nrows, V.J, nxt, bufs[b ^ 1]);
-        cp_async_wait<1>();
-      } else {
-        cp_async_wait<0>();
-      }
-      __syncthreads();
-      const int64_t n = tile * ST + threadIdx.x;
-      if (n < nrows) {
-        int ix, iy, iz;
-        decompose(g, n, ix, iy, iz);
-        const RowInfo R = row_info(g, ix, iy, iz);
-        const float* sv = bufs[b] + (int)(((uintptr_t)(V.J + seg[b]) & 15) / sizeof(float));
-        const float q = row_apply_f<1>(g, R, sv + (R.rp - seg[b]), V.p);
-        V.q[n] = q;
-        pq = fmaf(V.p[n], q, pq);
-      }
-      __syncthreads();
-      b ^= 1;
-    }
+    const bool ok = warp_staged_rows<float>(g, nrows, V.J, smem_raw, mbar, [&](int64_t n, const RowInfo& R,
+                                                                                const float* vals) {
+      fin(n, row_apply_f<1>(g, R, vals, V.z));
+    });
+    if (!ok) { V.s->status = MRG_ETIMEOUT; V.s->done = 1; }
   } else {
     for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
       int ix, iy, iz;
       decompose(g, n, ix, iy, iz);
-      const RowInfo R = row_info(g, ix, iy, iz);
-      const float q = row_apply_f<P>(g, R, V.J + R.rp, V.p);
-      V.q[n] = q;
-      pq = fmaf(V.p[n], q, pq);
+      const RowInfo R = row_info<P>(g, ix, iy, iz);
+      fin(n, row_apply_f<P>(g, R, V.J + R.rp, V.z));
     }
   }
   double m[1] = {block_sum((double)pq)};
@@ -639,21 +750,6 @@ __global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) 
   }
 }
 
-__global__ void __launch_bounds__(ST) k_pcg32_dir(int64_t nrows, PcgVec32 V) {
-  if (((volatile PcgScal*)V.s)->done) return;
-  const float beta = (float)V.s->beta;
-  const int64_t st = (int64_t)gridDim.x * ST;
-  int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
-  for (; n + 3 * st < nrows; n += 4 * st) {
-    float p[4], z[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) { p[k] = V.p[n + k * st]; z[k] = V.z[n + k * st]; }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) V.p[n + k * st] = fmaf(beta, p[k], z[k]);
-  }
-  for (; n < nrows; n += st) V.p[n] = fmaf(beta, V.p[n], V.z[n]);
-}
-
 // u += (double) du32   (mixed path update; Dirichlet rows have du = 0 because r = 0 there)
 __global__ void k_add_f32(int64_t n, const float* __restrict__ du, double* __restrict__ u) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -704,7 +800,7 @@ inline unsigned pcg_grid(const mrg_problem* p, int per_sm = 16) {
 
 // dynamic shared memory of the PCG SpMV: two staging buffers for P = 1
 template <int P, typename JT>
-constexpr int spmv_smem() { return P == 1 ? 2 * stage_elems<JT>() * (int)sizeof(JT) : 0; }
+constexpr int spmv_smem() { return P == 1 ? wspmv_smem<JT>() : 0; }
 // CTAs per SM the SpMV grid is sized for (shared-memory bound for P = 1)
 template <int P, typename JT>
 constexpr int spmv_per_sm() { return P == 1 ? (sizeof(JT) == 8 ? 4 : 7) : 16; }
@@ -801,7 +897,6 @@ static void enqueue_chunk32(const mrg_problem* p, const PcgVec32& V, cudaStream_
   for (int it = 0; it < CHUNK; ++it) {
     k_pcg32_spmv<P><<<nbs, ST, spmv_smem<P, float>(), s>>>(p->g, p->ndof, V);
     k_pcg32_update<<<nb, ST, 0, s>>>(p->ndof, V);
-    k_pcg32_dir<<<nb, ST, 0, s>>>(p->ndof, V);
   }
 }
 

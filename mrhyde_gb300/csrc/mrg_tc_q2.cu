@@ -1,85 +1,92 @@
-// Q2 Jacobian element contractions on the 5th-generation tensor cores (tcgen05, kind::tf32, 3xTF32).
+// Q2 element matrices on the 5th-generation tensor cores (tcgen05.mma kind::tf32, 3xTF32, operands
+// brought in by TMA, accumulators in TMEM, results written by TMA), then their deterministic row-gather
+// assembly into the CSR Jacobian.
 //
-// The row-gather Jacobian of the tensor-product path (mrg_assemble_q2.cu) is, for every (CSR row, cell)
-// pair m, one row of the product  D = A * B  with
-//     A[m][k]  = alpha_{d,q} = G_d[q][l] s_d^2 cw_q        (k = 27 d + q < 81)
-//              = beta_q      = sum_d G_d[q][l] ew_{q,d}      (k = 81 + q)
-//     B[k][j]  = [G_x; G_y; G_z; Phi][k][j]                  (constant, 108 x 27)
-// (l = local index of the row's node in the cell).  A CTA owns 32 consecutive CSR rows, enumerates their
-// (row, cell) pairs in a fixed order, builds A for up to 128 pairs at a time in shared memory, and one
-// thread issues tcgen05.mma (M = 128, N = 32, K = 8 per instruction, 14 K steps) into a 32-column TMEM
-// accumulator.  Each operand is split x = hi + lo with hi = x rounded to TF32, and D accumulates
-// A_hi B_hi + A_hi B_lo + A_lo B_hi in FP32 (3xTF32: ~2^-21 relative per product, i.e. FP32-class).
-// The accumulator rows are read back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pairs),
-// parked in shared memory, and each row's pairs are summed in a fixed order into the CTA's staged CSR
-// segment, which is written once with 16-byte stores.  The wait on the MMA completion mbarrier is
-// bounded; on time-out the kernel records an error, frees its TMEM and returns.
+// For one cell c of the tensor-product Q2 form (reference: src/physics/thermal.cpp:71-165 volume
+// residual, differentiated by the workset AD types of assemblyManager_jacres.hpp:121-630) the element
+// Jacobian is
+//     K_c[l][j] = sum_q cw_q sum_d s_d^2 G_d[q][l] G_d[q][j]  +  sum_{d,q} ew_{q,d} G_d[q][l] Phi[q][j]
+// with per-point coefficients W_c = (cw_q | ew_{q,x} | ew_{q,y} | ew_{q,z}) (108 values, written by the
+// residual pass; the ew block is zero for the linear thermal form) and the constant reference tables G_d
+// (gradients) and Phi (values).  All element matrices together are ONE GEMM with a constant right operand:
+//     E (ncell x 768) = W (ncell x K) * H (K x 768),   H[k][28 l + j] = the products above,
+// K = 108 (nonlinear) or 27 (thermal), the 27 x 27 element matrix stored with rows padded to 28 so that
+// each row starts on 16 bytes.  The GEMM runs in FP32-class precision as 3xTF32: every operand is split
+// x = hi + lo (hi = x rounded to TF32, lo = the rounded remainder) and E = Wh Hh + Wh Hl + Wl Hh.
 //
-// Operand layout: K-major, no swizzle.  A "core matrix" is 8 rows x 16 bytes (4 TF32 values); core
-// matrix (row group i, K chunk c) lives at byte (i * 28 + c) * 128, so the leading-dimension byte offset
-// (next core matrix along K) is 128 and the stride-dimension byte offset (next 8-row group) is 28 * 128.
-#include <cstdio>
+// k_q2_elem_tc is a persistent warp-specialised kernel (one CTA per SM, 6 warps):
+//   warp 0  producer: 1-D bulk copies (cp.async.bulk) of the 128-cell W tile (hi and lo planes) and of
+//           256-column slices of H in a 5-stage ring (K = 8 per stage).  Both operands are kept in global
+//           memory as the exact shared-memory image of the K-major no-swizzle core-matrix layout (the
+//           residual pass writes W that way; H is a constant built on the host), so each copy is one
+//           contiguous transfer instead of hundreds of 16-byte rows;
+//   warp 1  owns TMEM (512 columns = two 128 x 256 FP32 accumulators) and issues tcgen05.mma from one
+//           thread: per 256-column slice, K/8 steps x 3 products, then tcgen05.commit to the mbarriers
+//           that release the H stage, hand the accumulator to the epilogue and release the W tile;
+//   warps 2-5 epilogue: tcgen05.ld (warp w reads TMEM lanes 32 (w % 4) ..), stage 32 x 32 values in a
+//           128-byte-swizzled shared buffer (conflict-free) and write them with a TMA tensor store.
+// Every mbarrier wait is bounded by the global timer; on time-out the kernel raises a shared abort flag,
+// every role leaves its loop, waits (bounded) for its own copies and MMAs in flight, TMEM is freed and the
+// status word is set, so the host reports MRG_ETIMEOUT instead of hanging.
+//
+// k_q2_gather: one warp per CSR row, one lane per entry: J(i,j) = sum over the cells that contain both
+// nodes (fixed order cz, cy, cx) of E_c[l_i][l_j].  Every element-matrix value is read exactly once and
+// every Jacobian value is written exactly once, coalesced; no atomics, so the result is deterministic.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "mrg_device.cuh"
 #include "mrg_internal.h"
 
 namespace {
 
-constexpr int TCR = 32;                // CSR rows per work item
-constexpr int TCT = 128;               // threads per CTA (= M of one MMA tile)
-constexpr int KP = 112;                // K padded to a multiple of 8 (108 used)
-constexpr int NP = 32;                 // N padded (27 used)
-constexpr int KC = KP / 4;             // core-matrix columns along K
-constexpr int A_BYTES = TCT * KP * 4;  // 57344
-constexpr int B_BYTES = NP * KP * 4;   // 14336
-constexpr int TS = 28;                 // row stride of the plain FP32 table
-constexpr int MAXP = 8 * TCR;          // pairs per work item (8 cells per row at most)
+constexpr int TM = 128;           // cells per tile = MMA M
+constexpr int NE = 768;           // element-matrix columns (27 rows x 28 + 12 zero columns)
+constexpr int NCH = 256;          // columns per accumulator = MMA N
+constexpr int NNCH = NE / NCH;    // 3 accumulator slices per tile
+constexpr int KH = 112;           // H^T row length (K padded to a multiple of 8)
+constexpr int KW = 108;           // W row length in global memory
+constexpr int NBS = 5;            // H stages (K = 8 each)
+constexpr int A_PLANE = TM * KH * 4;          // 57344 bytes per W plane (hi or lo)
+constexpr int B_PLANE = NCH * 8 * 4;          // 8192 bytes per H plane per stage
+constexpr int B_STAGE = 2 * B_PLANE;          // hi + lo
+constexpr int E_BUF = 32 * 32 * 4;            // one epilogue staging buffer (32 cells x 32 columns)
+constexpr int THREADS = 192;
+constexpr int KSTEPS_MAX = KH / 8;            // 14
+constexpr int W_TILE_FLOATS = 2 * TM * KH;    // hi plane then lo plane of one 128-cell tile
+constexpr int H_STAGE_FLOATS = B_STAGE / 4;   // one (slice, K step) stage of H: hi chunks 0,1 then lo
 
-// shared-memory layout (bytes)
-constexpr int OFF_AHI = 0;
-constexpr int OFF_ALO = OFF_AHI + A_BYTES;
-constexpr int OFF_BHI = OFF_ALO + A_BYTES;
-constexpr int OFF_BLO = OFF_BHI + B_BYTES;
-constexpr int OFF_D = OFF_BLO + B_BYTES;              // float [128][28]
-constexpr int OFF_TAB = OFF_D + TCT * TS * 4;         // float [108][28]
-constexpr int OFF_SEG = OFF_TAB + 108 * TS * 4;       // float [TCR*125 + 4]
-constexpr int OFF_PAIR = OFF_SEG + (TCR * 125 + 4) * 4;  // int4 [MAXP]
-constexpr int OFF_MISC = OFF_PAIR + MAXP * 16;        // mbarrier (8) + tmem addr (4) + flags
-constexpr int TC_SMEM = OFF_MISC + 64;
+constexpr int OFF_AH = 0;
+constexpr int OFF_AL = OFF_AH + A_PLANE;
+constexpr int OFF_B = OFF_AL + A_PLANE;                 // NBS stages of [hi | lo]
+constexpr int OFF_E = OFF_B + NBS * B_STAGE;            // 4 warps x 2 buffers (1024-byte aligned)
+constexpr int OFF_BAR = OFF_E + 4 * 2 * E_BUF;
+// barriers: a_full, a_empty, b_full[NBS], b_empty[NBS], t_full[2], t_empty[2], spare
+constexpr int BAR_A_FULL = 0, BAR_A_EMPTY = 1, BAR_B_FULL = 2, BAR_B_EMPTY = 2 + NBS, BAR_T_FULL = 2 + 2 * NBS,
+              BAR_T_EMPTY = 4 + 2 * NBS, BAR_SPARE = 6 + 2 * NBS, NBAR = 7 + 2 * NBS;
+constexpr int OFF_MISC = OFF_BAR + NBAR * 8;            // tmem address (4) + abort flag (4)
+constexpr int SMEM_USED = OFF_MISC + 16;
+constexpr int SMEM_BYTES = SMEM_USED + 1024;            // slack for aligning the base to 1024 bytes
+static_assert(OFF_E % 1024 == 0, "swizzled staging buffers need 1024-byte alignment");
+static_assert(SMEM_BYTES <= 232448, "shared memory budget");
 
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// kind::tf32 instruction descriptor: D = F32, A = B = TF32, both K-major, N = 256, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NCH >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 
-// byte offset of (row, k) in the K-major no-swizzle core-matrix tile
-__device__ __forceinline__ uint32_t cm_off(int row, int k) {
-  return (uint32_t)(((row >> 3) * KC + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4);
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s: far above any legitimate wait
+
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
 }
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05; base offset 0, relative LBO, no swizzle
-  return d;
-}
-
-// kind::tf32 instruction descriptor: D = F32, A = B = TF32, both K-major, N = 32, M = 128
-constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) | ((uint32_t)(TCT >> 4) << 24);
-
-// round to the nearest TF32 value (10 explicit mantissa bits); the remainder x - hi is exact in FP32
-__device__ __forceinline__ float tf32_hi(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
@@ -89,276 +96,484 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: ~2^22 polls (well above the few microseconds an MMA batch takes)
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
-  for (int i = 0; i < (1 << 22); ++i)
-    if (mbar_try_wait(mbar, parity)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void decompose32(const Grid& g, int64_t n, int& ix, int& iy, int& iz) {
-  const unsigned un = (unsigned)n, nx = (unsigned)g.nn[0], ny = (unsigned)g.nn[1];
-  const unsigned t = un / nx;
-  ix = (int)(un - t * nx);
-  iy = (int)(t % ny);
-  iz = (int)(t / ny);
-}
-
-__device__ __forceinline__ int64_t rowptr2(const Grid& g, int ix, int iy, int iz, int& lx, int& ly, int& lz, int& cx,
-                                           int& cy, int& cz) {
-  axis_range(ix, g.nn[0], 2, lx, cx);
-  axis_range(iy, g.nn[1], 2, ly, cy);
-  axis_range(iz, g.nn[2], 2, lz, cz);
-  return g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
-}
-
-__device__ __forceinline__ int64_t rowptr_at2(const Grid& g, int64_t n, int64_t nrows) {
-  if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
-  int ix, iy, iz, a, b, c, d, e, f;
-  decompose32(g, n, ix, iy, iz);
-  return rowptr2(g, ix, iy, iz, a, b, c, d, e, f);
-}
-
-__global__ void __launch_bounds__(TCT, 1) k_q2_jac_tc(Grid g, int64_t nrows, int kind, float sq0, float sq1, float sq2,
-                                                      const float* __restrict__ tab_g, const float* __restrict__ qbuf,
-                                                      float* __restrict__ J, int ovw, int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  float* Dsm = reinterpret_cast<float*>(sm + OFF_D);
-  float* tab = reinterpret_cast<float*>(sm + OFF_TAB);
-  float* segbuf = reinterpret_cast<float*>(sm + OFF_SEG);
-  int4* pairs = reinterpret_cast<int4*>(sm + OFF_PAIR);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + OFF_MISC);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + OFF_MISC + 8);
-  int* s_flag = reinterpret_cast<int*>(sm + OFF_MISC + 12);
-  __shared__ int s_off[TCR + 1];
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const float sq[3] = {sq0, sq1, sq2};
-
-  // ---- one-time set-up: tables, B operand (hi/lo), mbarrier, TMEM ----
-  for (int k = t; k < 108 * TS; k += TCT) tab[k] = tab_g[k];
-  __syncthreads();
-  for (int e = t; e < NP * KP; e += TCT) {
-    const int j = e / KP, k = e % KP;
-    const float v = (j < 27 && k < 108) ? tab[k * TS + j] : 0.0f;
-    const float hi = tf32_hi(v);
-    *reinterpret_cast<float*>(sm + OFF_BHI + cm_off(j, k)) = hi;
-    *reinterpret_cast<float*>(sm + OFF_BLO + cm_off(j, k)) = v - hi;
+// Bounded wait on an mbarrier phase.  Returns false (and raises the CTA abort flag) on time-out, or
+// false when another role has already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, volatile int* abort_flag) {
+  if (mbar_try(mbar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try(mbar, parity)) return true;
+    if ((i & 63u) == 0) {
+      if (*abort_flag) return false;
+      if (gtimer() - t0 > WAIT_NS) {
+        *abort_flag = 1;
+        return false;
+      }
+    }
   }
-  if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(su32(mbar)) : "memory");
+}
+
+// wait with a limit only, used while cleaning up after an abort
+__device__ __forceinline__ void mbar_wait_cleanup(uint32_t mbar, uint32_t parity) {
+  const uint64_t t0 = gtimer();
+  while (!mbar_try(mbar, parity))
+    if (gtimer() - t0 > 200000000ull) return;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(src)
+               : "memory");
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // tcgen05 descriptor version; base offset 0, relative LBO, no swizzle
+  return d;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_q2_elem_tc(const float* __restrict__ wimg, const float* __restrict__ himg, const __grid_constant__ CUtensorMap mE,
+                 int ntiles, int ksteps, int* __restrict__ err) {
+  extern __shared__ unsigned char sm_raw[];
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(sm_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  unsigned char* sm = sm_raw + (base - raw);
+  const uint32_t sAh = base + OFF_AH, sAl = base + OFF_AL, sB = base + OFF_B, sE = base + OFF_E;
+  const uint32_t bar0 = base + OFF_BAR;
+  auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + OFF_MISC);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + OFF_MISC + 4);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar(BAR_A_FULL), 1);
+    mbar_init(bar(BAR_A_EMPTY), 1);
+    for (int s = 0; s < NBS; ++s) {
+      mbar_init(bar(BAR_B_FULL + s), 1);
+      mbar_init(bar(BAR_B_EMPTY + s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(bar(BAR_T_FULL + b), 1);
+      mbar_init(bar(BAR_T_EMPTY + b), 4);
+    }
+    mbar_init(bar(BAR_SPARE), 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    *s_flag = 0;
+    *abort_flag = 0;
   }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(su32(tmem_slot))
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(tmem_slot))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t dtmem = *tmem_slot;
-  uint32_t phase = 0;
-  bool failed = false;
+  const uint32_t tmem = *tmem_slot;
+  const int kchunks = 2 * ksteps;  // 16-byte K chunks of W per tile
 
-  const int64_t nchunks = (nrows + TCR - 1) / TCR;
-  for (int64_t ch = blockIdx.x; ch < nchunks && !failed; ch += gridDim.x) {
-    const int64_t n0 = ch * TCR;
-    const int64_t n1 = (n0 + TCR < nrows) ? n0 + TCR : nrows;
-    const int64_t seg0 = rowptr_at2(g, n0, nrows), seg1 = rowptr_at2(g, n1, nrows);
-    const int phs = (int)(((uintptr_t)(J + seg0) & 15) / sizeof(float));
-    float* sv = segbuf + phs;
-    for (int64_t k = t; k < seg1 - seg0; k += TCT) sv[k] = 0.0f;
-    // row descriptors (threads 0..TCR-1)
-    int64_t rp = 0, diag = 0;
-    int lx = 0, ly = 0, lz = 0, cxn = 0, cyn = 0, czn = 0, fx = 0, fy = 0, fz = 0, nxc = 0, nyc = 0, nzc = 0;
-    int ix = 0, iy = 0, iz = 0, npair = 0;
-    bool fixed = false, act = false;
-    if (t < TCR) {
-      const int64_t n = n0 + t;
-      act = n < nrows;
-      if (act) {
-        decompose32(g, n, ix, iy, iz);
-        rp = rowptr2(g, ix, iy, iz, lx, ly, lz, cxn, cyn, czn);
-        diag = ((int64_t)(iz - lz) * cyn + (iy - ly)) * cxn + (ix - lx);
-        fixed = node_fixed(g, ix, iy, iz);
-        if (!fixed) {
-          axis_cells(ix, g.nn[0], 2, fx, nxc);
-          axis_cells(iy, g.nn[1], 2, fy, nyc);
-          axis_cells(iz, g.nn[2], 2, fz, nzc);
-          npair = nxc * nyc * nzc;
-        }
-      }
-      // exclusive scan of the pair counts over warp 0
-      int incl = npair;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-      }
-      s_off[t] = incl - npair;
-      if (t == TCR - 1) s_off[TCR] = incl;
-    }
-    __syncthreads();
-    if (t < TCR && npair) {
-      int m = s_off[t];
-      for (int ccz = fz; ccz < fz + nzc; ++ccz)
-        for (int ccy = fy; ccy < fy + nyc; ++ccy)
-          for (int ccx = fx; ccx < fx + nxc; ++ccx) {
-            const int l = (ix - 2 * ccx) + 3 * (iy - 2 * ccy) + 9 * (iz - 2 * ccz);
-            const int cid = ccx + g.nc[0] * (ccy + g.nc[1] * ccz);
-            pairs[m++] = make_int4(t, cid, l, ccx | (ccy << 10) | (ccz << 20));
+  if (warp == 0) {
+    // ------------------------------ TMA producer ------------------------------
+    if (lane == 0) {
+      bool ok = true;
+      uint32_t bit = 0, ta = 0;
+      int a_armed = -1;
+      int b_armed[NBS];
+      for (int s = 0; s < NBS; ++s) b_armed[s] = -1;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++ta) {
+        if (!mbar_wait(bar(BAR_A_EMPTY), (ta & 1u) ^ 1u, abort_flag)) { ok = false; break; }
+        const uint32_t abytes = (uint32_t)(kchunks * TM * 16);
+        mbar_expect_tx(bar(BAR_A_FULL), 2u * abytes);
+        a_armed = (int)(ta & 1u);
+        const float* wt = wimg + (size_t)tile * W_TILE_FLOATS;
+        bulk_load(sAh, wt, abytes, bar(BAR_A_FULL));
+        bulk_load(sAl, wt + TM * KH, abytes, bar(BAR_A_FULL));
+        for (int n = 0; n < NNCH && ok; ++n)
+          for (int ks = 0; ks < ksteps; ++ks, ++bit) {
+            const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
+            if (!mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag)) { ok = false; break; }
+            mbar_expect_tx(bar(BAR_B_FULL + st), (uint32_t)B_STAGE);
+            b_armed[st] = (int)ph;
+            bulk_load(sB + st * B_STAGE, himg + (size_t)(n * KSTEPS_MAX + ks) * H_STAGE_FLOATS, (uint32_t)B_STAGE,
+                      bar(BAR_B_FULL + st));
           }
-    }
-    __syncthreads();
-    const int ptotal = s_off[TCR];
-    for (int base = 0; base < ptotal; base += TCT) {
-      // ---- build A rows (hi/lo) for pairs base..base+127 ----
-      const int m = base + t;
-      if (m < ptotal) {
-        const int4 pr = pairs[m];
-        const int l = pr.z;
-        const float* qb = qbuf + (int64_t)pr.y * 108;
-        for (int k = 0; k < KP; ++k) {
-          float v = 0.0f;
-          if (k < 81) {
-            const int d = k / 27, q = k % 27;
-            v = tab[k * TS + l] * sq[d] * __ldg(qb + q);
-          } else if (k < 108 && kind != MRG_THERMAL) {
-            const int q = k - 81;
-            v = tab[q * TS + l] * __ldg(qb + 27 + q) + tab[(27 + q) * TS + l] * __ldg(qb + 54 + q) +
-                tab[(54 + q) * TS + l] * __ldg(qb + 81 + q);
-          }
-          const float hi = tf32_hi(v);
-          *reinterpret_cast<float*>(sm + OFF_AHI + cm_off(t, k)) = hi;
-          *reinterpret_cast<float*>(sm + OFF_ALO + cm_off(t, k)) = v - hi;
-        }
-      } else {
-        for (int k = 0; k < KP; ++k) {
-          *reinterpret_cast<float*>(sm + OFF_AHI + cm_off(t, k)) = 0.0f;
-          *reinterpret_cast<float*>(sm + OFF_ALO + cm_off(t, k)) = 0.0f;
+      }
+      if (ok) {
+        // tail: wait until the MMA thread has released every stage, so that no arrive lands after exit
+        for (int s = 0; s < NBS && ok; ++s, ++bit) {
+          const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
+          if (b_armed[st] >= 0 && !mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag)) ok = false;
         }
       }
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      __syncthreads();
-      // ---- one thread issues the 3xTF32 MMAs ----
-      if (t == 0) {
+      if (!ok) {
+        // copies in flight land on their full barriers: wait for the last phase armed on each
+        if (a_armed >= 0) mbar_wait_cleanup(bar(BAR_A_FULL), (uint32_t)a_armed);
+        for (int s = 0; s < NBS; ++s)
+          if (b_armed[s] >= 0) mbar_wait_cleanup(bar(BAR_B_FULL + s), (uint32_t)b_armed[s]);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ------------------------------ MMA issuer ------------------------------
+    if (lane == 0) {
+      bool ok = true, issued = false;
+      uint32_t bit = 0, acc = 0, ta = 0;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++ta) {
+        if (!mbar_wait(bar(BAR_A_FULL), ta & 1u, abort_flag)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const uint32_t ahi = su32(sm + OFF_AHI), alo = su32(sm + OFF_ALO);
-        const uint32_t bhi = su32(sm + OFF_BHI), blo = su32(sm + OFF_BLO);
-        for (int ks = 0; ks < KP / 8; ++ks) {
-          const uint32_t koff = (uint32_t)ks * 256u;  // two core-matrix columns per K step
-          const uint64_t dAh = smem_desc(ahi + koff, 128, KC * 128), dAl = smem_desc(alo + koff, 128, KC * 128);
-          const uint64_t dBh = smem_desc(bhi + koff, 128, KC * 128), dBl = smem_desc(blo + koff, 128, KC * 128);
-          mma_tf32(dtmem, dAh, dBh, ks > 0 ? 1u : 0u);
-          mma_tf32(dtmem, dAh, dBl, 1u);
-          mma_tf32(dtmem, dAl, dBh, 1u);
+        for (int n = 0; n < NNCH && ok; ++n, ++acc) {
+          const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
+          if (!mbar_wait(bar(BAR_T_EMPTY + buf), aph ^ 1u, abort_flag)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t d = tmem + buf * NCH;
+          for (int ks = 0; ks < ksteps; ++ks, ++bit) {
+            const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
+            if (!mbar_wait(bar(BAR_B_FULL + st), ph, abort_flag)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t bh = sB + st * B_STAGE, bl = bh + B_PLANE;
+            const uint32_t koff = (uint32_t)ks * 2u * (TM * 16);
+            const uint64_t dAh = smem_desc(sAh + koff, TM * 16, 128), dAl = smem_desc(sAl + koff, TM * 16, 128);
+            const uint64_t dBh = smem_desc(bh, NCH * 16, 128), dBl = smem_desc(bl, NCH * 16, 128);
+            mma_tf32(d, dAh, dBh, ks > 0 ? 1u : 0u);
+            mma_tf32(d, dAh, dBl, 1u);
+            mma_tf32(d, dAl, dBh, 1u);
+            issued = true;
+            mma_commit(bar(BAR_B_EMPTY + st));
+          }
+          if (ok) mma_commit(bar(BAR_T_FULL + buf));
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(su32(mbar))
-                     : "memory");
+        if (ok && tile + (int)gridDim.x < ntiles) mma_commit(bar(BAR_A_EMPTY));
       }
-      if (!mbar_wait_bounded(su32(mbar), phase)) atomicExch(s_flag, 1);
-      phase ^= 1u;
-      __syncthreads();
-      if (*s_flag) {
-        failed = true;
-        break;
+      if (!ok && issued) {
+        // let the MMAs already issued finish before TMEM is released
+        mma_commit(bar(BAR_SPARE));
+        mbar_wait_cleanup(bar(BAR_SPARE), 0u);
       }
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      // ---- accumulator rows back to registers (warp w: TMEM lanes 32w..32w+31) ----
-      uint32_t r[32];
-      const uint32_t taddr = dtmem + ((uint32_t)(warp * 32) << 16);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-          : "r"(taddr)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------ epilogue (warps 2..5) ------------------------------
+    const int q = warp & 3;           // TMEM lane quarter this warp may access
+    const int ew = warp - 2;          // staging buffers of this warp
+    const uint32_t stg0 = sE + (uint32_t)ew * 2u * E_BUF;
+    bool ok = true;
+    uint32_t acc = 0, piece = 0;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int row0 = tile * TM + 32 * q;
+      for (int n = 0; n < NNCH; ++n, ++acc) {
+        const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
+        int good = 1;
+        if (lane == 0) good = mbar_wait(bar(BAR_T_FULL + buf), aph, abort_flag) ? 1 : 0;
+        good = __shfl_sync(0xffffffffu, good, 0);
+        if (!good) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        for (int p = 0; p < NCH / 32; ++p, ++piece) {
+          uint32_t r[32];
+          const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * NCH + 32u * (uint32_t)p;
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+              : "r"(taddr)
+              : "memory");
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          const uint32_t stg = stg0 + (piece & 1u) * E_BUF;
+          // the store issued from this buffer two pieces ago must have finished reading it
+          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
+          __syncwarp();
+          // row = lane (128 bytes); 16-byte chunk c goes to chunk position c ^ (row & 7) (128B swizzle)
 #pragma unroll
-      for (int j = 0; j < 27; ++j) Dsm[t * TS + j] = __uint_as_float(r[j]);
-      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      __syncthreads();
-      // ---- each row sums its pairs of this tile in order into its staged CSR row ----
-      if (t < TCR && act && !fixed) {
-        const int p0 = max(s_off[t], base), p1 = min(s_off[t + 1], base + TCT);
-        float* row = sv + (rp - seg0);
-        for (int pm = p0; pm < p1; ++pm) {
-          const int4 pr = pairs[pm];
-          const int ccx = pr.w & 1023, ccy = (pr.w >> 10) & 1023, ccz = pr.w >> 20;
-          const float* dr = Dsm + (pm - base) * TS;
-#pragma unroll
-          for (int j = 0; j < 27; ++j) {
-            const int jx = 2 * ccx + j % 3, jy = 2 * ccy + (j / 3) % 3, jz = 2 * ccz + j / 9;
-            row[((int64_t)(jz - lz) * cyn + (jy - ly)) * cxn + (jx - lx)] += dr[j];
+          for (int c = 0; c < 8; ++c) {
+            const uint32_t a = stg + (uint32_t)lane * 128u + (uint32_t)((c ^ (lane & 7)) << 4);
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(a), "r"(r[4 * c]), "r"(r[4 * c + 1]),
+                         "r"(r[4 * c + 2]), "r"(r[4 * c + 3])
+                         : "memory");
+          }
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_2d(&mE, n * NCH + 32 * p, row0, stg);
+            asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
           }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar(BAR_T_EMPTY + buf));
       }
-      __syncthreads();
     }
-    if (failed) break;
-    if (t < TCR && act && fixed && ovw) sv[(rp - seg0) + diag] = 1.0f;
-    __syncthreads();
-    // ---- write the segment once (16-byte stores), or add into it ----
-    {
-      float* dst = J + seg0;
-      const int64_t len = seg1 - seg0;
-      int head = (int)(((16 - ((uintptr_t)dst & 15)) & 15) / 4);
-      if (head > len) head = (int)len;
-      for (int k = t; k < head; k += TCT) dst[k] = ovw ? sv[k] : dst[k] + sv[k];
-      const int64_t body = (len - head) / 4;
-      const float4* s4 = reinterpret_cast<const float4*>(sv + head);
-      float4* d4 = reinterpret_cast<float4*>(dst + head);
-      for (int64_t v = t; v < body; v += TCT) {
-        float4 x = s4[v];
-        if (!ovw) {
-          const float4 y = d4[v];
-          x.x += y.x; x.y += y.y; x.z += y.z; x.w += y.w;
-        }
-        __stcs(d4 + v, x);
-      }
-      for (int64_t k = head + body * 4 + t; k < len; k += TCT) dst[k] = ovw ? sv[k] : dst[k] + sv[k];
-    }
-    if (!ovw) {
-      __syncthreads();
-      if (t < TCR && act && fixed) J[rp + diag] = 1.0f;
-    }
-    __syncthreads();
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+    __syncwarp();
   }
-  if (failed && t == 0) atomicExch(err, 1);
-  // ---- release TMEM ----
+
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
-  if (warp == 0) {
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 1);
+  if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(dtmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem) : "memory");
   }
+}
+
+// cells along one axis that contain both node i and node j (p = 2): [lo, hi]
+__device__ __forceinline__ void pair_cells(int i, int j, int nc, int& lo, int& hi) {
+  const int mn = i < j ? i : j, mx = i < j ? j : i;
+  lo = (mx - 1) >> 1;
+  if (lo < 0) lo = 0;
+  hi = mn >> 1;
+  if (hi > nc - 1) hi = nc - 1;
+}
+
+constexpr int GT = 256;  // gather threads per CTA (8 rows in flight)
+
+// One warp per CSR row.  Lane l < 27 stands for local column node l of a cell: for each of the row's
+// cells (at most 8, in the fixed order cz, cy, cx) it loads E_c[l_i][l] -- a contiguous run of 27 values
+// -- and adds it to the row's entry of that column in a per-warp shared row.  All loads of a row are
+// issued before the first add; the adds are ordered by cell, so every entry is summed in the same fixed
+// order on every run.  The row is then written once, coalesced.
+__global__ void __launch_bounds__(GT) k_q2_gather(Grid g, int64_t nrows, const float* __restrict__ E,
+                                                  float* __restrict__ J, int ovw) {
+  __shared__ float rows[GT / 32][128];
+  const int lane = threadIdx.x & 31;
+  float* rb = rows[threadIdx.x >> 5];
+  const int64_t wid = ((int64_t)blockIdx.x * GT + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * GT) >> 5;
+  const int ncx = g.nc[0], ncy = g.nc[1];
+  const bool col = lane < 27;
+  const int ljx = lane % 3, ljy = (lane / 3) % 3, ljz = lane / 9;
+  for (int64_t n = wid; n < nrows; n += nw) {
+    int ix, iy, iz;
+    mrgdev::decompose(g, n, ix, iy, iz);
+    const mrgdev::RowInfo R = mrgdev::row_info<2>(g, ix, iy, iz);
+    const int len = R.cx * R.cy * R.cz;
+    float* row = J + R.rp;
+    if (node_fixed(g, ix, iy, iz)) {
+      const int dg = (int)(mrgdev::diag_pos(R, ix, iy, iz) - R.rp);
+      if (ovw) {
+        for (int e = lane; e < len; e += 32) __stcs(row + e, e == dg ? 1.0f : 0.0f);
+      } else if (lane == 0) {
+        row[dg] = 1.0f;
+      }
+      continue;
+    }
+    int fx, fy, fz, nxc, nyc, nzc;
+    axis_cells(ix, g.nn[0], 2, fx, nxc);
+    axis_cells(iy, g.nn[1], 2, fy, nyc);
+    axis_cells(iz, g.nn[2], 2, fz, nzc);
+    const int ncells = nxc * nyc * nzc;
+    // cell (fx+kx, fy+ky, fz+kz): local row index li0 - 2 (kx + 3 ky + 9 kz), row position of this
+    // lane's column pos0 + 2 (kz cy cx + ky cx + kx), cell index cell0 + kx + ncx (ky + ncy kz)
+    const int li0 = (ix - 2 * fx) + 3 * (iy - 2 * fy) + 9 * (iz - 2 * fz);
+    const int pos0 = ((2 * fz + ljz - R.lz) * R.cy + (2 * fy + ljy - R.ly)) * R.cx + (2 * fx + ljx - R.lx);
+    const float* e0 = E + (fx + (int64_t)ncx * (fy + (int64_t)ncy * fz)) * NE + lane;
+    const int64_t sy = (int64_t)ncx * NE, sz = (int64_t)ncx * ncy * NE;
+    float v[8];
+    int pos[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      // k -> (kx, ky, kz), x fastest
+      const int kx = (nxc == 2) ? (k & 1) : 0, k2 = (nxc == 2) ? (k >> 1) : k;
+      const int ky = (nyc == 2) ? (k2 & 1) : 0, kz = (nyc == 2) ? (k2 >> 1) : k2;
+      const int li = li0 - 2 * (kx + 3 * ky + 9 * kz);
+      const bool on = col && k < ncells;
+      v[k] = on ? __ldg(e0 + kx * NE + ky * sy + kz * sz + li * 28) : 0.0f;
+      pos[k] = pos0 + 2 * ((kz * R.cy + ky) * R.cx + kx);
+    }
+    for (int e = lane; e < len; e += 32) rb[e] = 0.0f;
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < ncells) {
+        if (col) rb[pos[k]] += v[k];
+        __syncwarp();
+      }
+    }
+    for (int e = lane; e < len; e += 32) {
+      if (ovw) __stcs(row + e, rb[e]); else row[e] += rb[e];
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+int make_map(CUtensorMap* m, const void* gaddr, uint64_t inner, uint64_t outer, uint64_t row_bytes, uint32_t box_in,
+             uint32_t box_out, CUtensorMapSwizzle sw) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return mrg_fail(MRG_ECUDA, "cuTensorMapEncodeTiled entry point not available");
+  const cuuint64_t dims[2] = {inner, outer};
+  const cuuint64_t strides[1] = {row_bytes};
+  const cuuint32_t box[2] = {box_in, box_out};
+  const cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(gaddr), dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    char b[160];
+    snprintf(b, sizeof b, "cuTensorMapEncodeTiled failed (%d) for a %llu x %llu map", (int)r,
+             (unsigned long long)inner, (unsigned long long)outer);
+    return mrg_fail(MRG_ECUDA, b);
+  }
+  return MRG_OK;
+}
+
+// TF32 with round-to-nearest (ties away from zero), host side: 10 explicit mantissa bits
+float tf32_round_host(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+  float y;
+  memcpy(&y, &u, 4);
+  return y;
 }
 
 }  // namespace
 
-// Launches the tensor-core Jacobian for a Q2 problem.  tab32 = [G_x | G_y | G_z | Phi] rows of 28 floats,
-// qbuf = per-cell FP32 coefficients (cw, ew) written by the residual pass, err = device int (0 on entry).
-int mrg_launch_q2_jac_tc(const mrg_problem* p, const float* tab32, const float* qbuf, float* J, bool ovw, int* err,
-                         double s0, double s1, double s2, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_q2_jac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    if (e != cudaSuccess) return mrg_cuda_check(e, "tensor-core Jacobian smem attribute");
-    attr = true;
-  }
+struct Q2Tc {
+  CUtensorMap mE;
+  float* d_w = nullptr;   // W image: [tile][hi, lo][K chunk 28][cell 128][4]
+  float* d_h = nullptr;   // H image: [slice 3][K step 14][hi, lo][K chunk 2][column 256][4]
+  float* d_e = nullptr;   // [ntiles * 128][768] element matrices
+  int ntiles = 0, ksteps = 0;
+};
+
+// Builds H^T (hi/lo) from the reference tables tab[(d*27 + q)*28 + j] (d = 0..2 gradients, 3 = values)
+// and the axis scalings s[d] = 2 / h_d, allocates the coefficient and element buffers and encodes the
+// tensor maps.  W is written by the residual pass into q2tc_w_planes().
+int mrg_q2tc_create(mrg_problem* p, const double* tab, const double s[3], Q2Tc** out, cudaStream_t st) {
+  Q2Tc* T = new Q2Tc();
+  const bool thermal = p->kind == MRG_THERMAL;
+  T->ntiles = (int)((p->ncell + TM - 1) / TM);
+  T->ksteps = thermal ? 4 : KH / 8;
+  std::vector<float> h((size_t)NNCH * KSTEPS_MAX * H_STAGE_FLOATS, 0.0f);
+  // position of H^T[n][k] (plane 0 = hi, 1 = lo) in the stage image
+  auto at = [&](int n, int k, int plane) {
+    const int sl = n / NCH, col = n % NCH, ks = k / 8, c = (k % 8) / 4;
+    return (size_t)(sl * KSTEPS_MAX + ks) * H_STAGE_FLOATS + (size_t)plane * (B_PLANE / 4) + (size_t)c * NCH * 4 +
+           (size_t)col * 4 + (size_t)(k % 4);
+  };
+  auto G = [&](int d, int q, int j) { return tab[(d * 27 + q) * 28 + j]; };
+  for (int l = 0; l < 27; ++l)
+    for (int j = 0; j < 27; ++j) {
+      const int n = 28 * l + j;
+      for (int k = 0; k < KW; ++k) {
+        double v;
+        if (k < 27) {
+          v = 0.0;
+          for (int d = 0; d < 3; ++d) v += s[d] * s[d] * G(d, k, l) * G(d, k, j);
+        } else {
+          const int d = (k - 27) / 27, q = (k - 27) % 27;
+          v = G(d, q, l) * G(3, q, j);
+        }
+        const float hi = tf32_round_host((float)v);
+        h[at(n, k, 0)] = hi;
+        h[at(n, k, 1)] = tf32_round_host((float)(v - (double)hi));
+      }
+    }
+  auto fail = [&](int rc) {
+    if (T->d_w) cudaFreeAsync(T->d_w, st);
+    if (T->d_h) cudaFreeAsync(T->d_h, st);
+    if (T->d_e) cudaFreeAsync(T->d_e, st);
+    delete T;
+    return rc;
+  };
+  const size_t wbytes = (size_t)T->ntiles * W_TILE_FLOATS * sizeof(float);
+  cudaError_t e = cudaMallocAsync(&T->d_w, wbytes, st);
+  // slots never written by the residual pass (K padding, the ew block of the thermal form, cells past
+  // the end of the last tile) must read as zero
+  if (e == cudaSuccess) e = cudaMemsetAsync(T->d_w, 0, wbytes, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&T->d_h, h.size() * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&T->d_e, (size_t)T->ntiles * TM * NE * sizeof(float), st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(T->d_h, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return fail(mrg_cuda_check(e, "tensor-core Q2 buffers"));
+  int rc = make_map(&T->mE, T->d_e, NE, (uint64_t)T->ntiles * TM, NE * 4, 32, 32, CU_TENSOR_MAP_SWIZZLE_128B);
+  if (rc) return fail(rc);
+  *out = T;
+  return MRG_OK;
+}
+
+void mrg_q2tc_free(Q2Tc* T, cudaStream_t st) {
+  if (!T) return;
+  cudaFreeAsync(T->d_w, st);
+  cudaFreeAsync(T->d_h, st);
+  cudaFreeAsync(T->d_e, st);
+  delete T;
+}
+
+float* mrg_q2tc_w_image(Q2Tc* T) { return T->d_w; }
+
+// Element matrices (tensor cores) then the row gather into J (FP32 values of the canonical graph).
+int mrg_q2tc_launch(const mrg_problem* p, Q2Tc* T, float* J, bool ovw, int* err, cudaStream_t s) {
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_q2_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
+  if (attr_err != cudaSuccess) return mrg_cuda_check(attr_err, "tensor-core element kernel smem attribute");
   int dev = 0, nsm = 0;
   MRG_CUDA(cudaGetDevice(&dev));
   MRG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t nchunks = (p->ndof + TCR - 1) / TCR;
-  const int grid = (int)((nchunks < nsm) ? nchunks : nsm);
-  k_q2_jac_tc<<<grid, TCT, TC_SMEM, s>>>(p->g, p->ndof, p->kind, (float)(s0 * s0), (float)(s1 * s1), (float)(s2 * s2),
-                                         tab32, qbuf, J, ovw ? 1 : 0, err);
+  const int grid = T->ntiles < nsm ? T->ntiles : nsm;
+  k_q2_elem_tc<<<grid, THREADS, SMEM_BYTES, s>>>(T->d_w, T->d_h, T->mE, T->ntiles, T->ksteps, err);
   cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "tensor-core Jacobian launch");
+  if (e != cudaSuccess) return mrg_cuda_check(e, "tensor-core element kernel launch");
+  const int64_t warps_needed = p->ndof;
+  int64_t blocks = (warps_needed * 32 + GT - 1) / GT;
+  if (blocks > (int64_t)nsm * 16) blocks = (int64_t)nsm * 16;
+  k_q2_gather<<<(unsigned)blocks, GT, 0, s>>>(p->g, p->ndof, T->d_e, J, ovw ? 1 : 0);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "element gather launch");
 }
 
-int mrg_tc_smem_bytes() { return TC_SMEM; }
+int mrg_tc_smem_bytes() { return SMEM_BYTES; }

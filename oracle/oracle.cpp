@@ -26,6 +26,9 @@
 //   * Gauss rule of order 2p  src/interfaces/discretization/discretizationInterface_construct.hpp:111
 //                             src/interfaces/discretization/discretizationInterface_integration.hpp:91-104
 //   * Lagrange HGRAD bases    src/interfaces/discretization/discretizationInterface_basis.hpp:219-260
+//   * boundary terms          src/physics/thermal.cpp:170-260 (Neumann, weak Dirichlet), side element
+//                             size src/tools/workset.cpp:2719-2733, boundary workset loop
+//                             src/managers/assembly/assemblyManager_jacres.hpp:485-603
 //
 // Third-party arithmetic the reference delegates (not vendored in the reference tree, versions
 // unpinned beyond Trilinos >= 14): Intrepid2 HGRAD_{QUAD,HEX}_{C1,Cn} Lagrange bases, Gauss-Legendre
@@ -192,6 +195,9 @@ struct orc_problem {
   std::vector<double> dpsi;      // [nvpe*nq*dim]
   std::vector<double> qxi;       // [nq*dim]
   int ws;
+  int qorder;                    // 1-D Gauss order of the volume rule (the side rule uses the same)
+  int bc_kind[6] = {0, 0, 0, 0, 0, 0};  // per face: 0 none, 1 Neumann, 2 weak Dirichlet
+  std::vector<double> bc_g[6];          // per face: boundary data at the side points (face order)
 };
 
 namespace {
@@ -375,6 +381,222 @@ void assemble_cell(const orc_problem* P, int64_t c, const double* u, double* r, 
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// Boundary terms (thermal.cpp:170-260).  Face f = 2a + s: a = normal axis, s = 0 (low) / 1 (high).
+// Side points: the volume rule's 1-D Gauss points on the tangential axes (first tangential axis
+// fastest), xi_a = -1 or +1.  Face cells are ordered by their tangential cell coordinates (first
+// tangential axis fastest); the boundary data of a face is one value per (face cell, side point).
+// ------------------------------------------------------------------------------------------
+void side_rule(const orc_problem* P, int face, std::vector<double>& xi, std::vector<double>& wr) {
+  std::vector<double> gx, gw;
+  gauss_legendre(P->qorder, gx, gw);
+  const int n1 = (int)gx.size(), d = P->dim, a = face / 2;
+  int t[2] = {-1, -1}, nt = 0;
+  for (int k = 0; k < d; ++k)
+    if (k != a) t[nt++] = k;
+  const int npts = (d == 3) ? n1 * n1 : n1;
+  xi.assign((size_t)npts * d, 0.0);
+  wr.assign(npts, 1.0);
+  for (int q = 0; q < npts; ++q) {
+    const int i0 = q % n1, i1 = q / n1;
+    xi[(size_t)q * d + a] = (face % 2) ? 1.0 : -1.0;
+    xi[(size_t)q * d + t[0]] = gx[i0];
+    wr[q] = gw[i0];
+    if (d == 3) {
+      xi[(size_t)q * d + t[1]] = gx[i1];
+      wr[q] *= gw[i1];
+    }
+  }
+}
+
+std::vector<int64_t> face_cells(const orc_problem* P, int face) {
+  const int d = P->dim, a = face / 2;
+  const int nc[3] = {P->nx, P->ny, P->nz};
+  int t[2] = {-1, -1}, nt = 0;
+  for (int k = 0; k < d; ++k)
+    if (k != a) t[nt++] = k;
+  const int n0 = nc[t[0]], n1 = (d == 3) ? nc[t[1]] : 1;
+  std::vector<int64_t> out;
+  out.reserve((size_t)n0 * n1);
+  for (int j = 0; j < n1; ++j)
+    for (int i = 0; i < n0; ++i) {
+      int cc[3] = {0, 0, 0};
+      cc[a] = (face % 2) ? nc[a] - 1 : 0;
+      cc[t[0]] = i;
+      if (d == 3) cc[t[1]] = j;
+      out.push_back(cc[0] + (int64_t)P->nx * (cc[1] + (int64_t)P->ny * cc[2]));
+    }
+  return out;
+}
+
+// Cell c at the side points of `face`: coordinates x, basis values phi [npe][npts], physical gradients
+// gphys [npe][npts][dim], weights w = w_ref * side measure, outward unit normal nrm [npts][dim].
+// (CellTools Jacobian; side measure |dx/dxi_t| (2-D) or |dx/dxi_t1 x dx/dxi_t2| (3-D); normal
+// +-J^{-T} e_a normalised.)
+void side_geometry(const orc_problem* P, int64_t c, int face, const std::vector<double>& xi,
+                   const std::vector<double>& wr, double* x, double* phi, double* gphys, double* w, double* nrm) {
+  const int d = P->dim, p = P->p, a = face / 2;
+  const int npts = (int)wr.size();
+  double xv[8][3];
+  for (int v = 0; v < P->nvpe; ++v) {
+    const int vid = P->cverts[c * P->nvpe + v];
+    for (int k = 0; k < d; ++k) xv[v][k] = P->vcoord[(int64_t)vid * d + k];
+  }
+  std::vector<double> l(p + 1), dl(p + 1);
+  for (int q = 0; q < npts; ++q) {
+    const double* e = &xi[(size_t)q * d];
+    double L[3][8], DL[3][8], G[3][2], DG[3][2];
+    double l1[2], dl1[2];
+    for (int k = 0; k < d; ++k) {
+      lagrange1d(p, e[k], l.data(), dl.data());
+      for (int b = 0; b <= p; ++b) { L[k][b] = l[b]; DL[k][b] = dl[b]; }
+      lagrange1d(1, e[k], l1, dl1);
+      for (int b = 0; b < 2; ++b) { G[k][b] = l1[b]; DG[k][b] = dl1[b]; }
+    }
+    double J[3][3] = {{0}};
+    for (int k = 0; k < d; ++k) x[q * d + k] = 0.0;
+    for (int v = 0; v < P->nvpe; ++v) {
+      const int av[3] = {v % 2, (v / 2) % 2, v / 4};
+      double ps = 1.0;
+      for (int k = 0; k < d; ++k) ps *= G[k][av[k]];
+      for (int k = 0; k < d; ++k) {
+        x[q * d + k] += xv[v][k] * ps;
+        for (int gg = 0; gg < d; ++gg) {
+          double dp = 1.0;
+          for (int m = 0; m < d; ++m) dp *= (m == gg) ? DG[m][av[m]] : G[m][av[m]];
+          J[k][gg] += xv[v][k] * dp;
+        }
+      }
+    }
+    double det, Ji[3][3];
+    if (d == 2) {
+      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+      Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+    } else {
+      det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+            J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+      Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+      Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+      Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+      Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+      Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+      Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+      Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+      Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    }
+    // side measure from the tangential columns of J
+    int t[2] = {-1, -1}, nt = 0;
+    for (int k = 0; k < d; ++k)
+      if (k != a) t[nt++] = k;
+    double meas;
+    if (d == 2) {
+      meas = std::sqrt(J[0][t[0]] * J[0][t[0]] + J[1][t[0]] * J[1][t[0]]);
+    } else {
+      const double u0[3] = {J[0][t[0]], J[1][t[0]], J[2][t[0]]}, u1[3] = {J[0][t[1]], J[1][t[1]], J[2][t[1]]};
+      const double cr[3] = {u0[1] * u1[2] - u0[2] * u1[1], u0[2] * u1[0] - u0[0] * u1[2], u0[0] * u1[1] - u0[1] * u1[0]};
+      meas = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    }
+    w[q] = wr[q] * meas;
+    double nv[3], nn2 = 0.0;
+    for (int k = 0; k < d; ++k) { nv[k] = Ji[a][k]; nn2 += nv[k] * nv[k]; }
+    const double sgn = (face % 2) ? 1.0 : -1.0, inv = sgn / std::sqrt(nn2);
+    for (int k = 0; k < d; ++k) nrm[q * d + k] = nv[k] * inv;
+    for (int i = 0; i < P->npe; ++i) {
+      const int ai[3] = {i % (p + 1), (i / (p + 1)) % (p + 1), (d == 3) ? i / ((p + 1) * (p + 1)) : 0};
+      double v = 1.0, dr[3];
+      for (int k = 0; k < d; ++k) v *= L[k][ai[k]];
+      for (int gg = 0; gg < d; ++gg) {
+        double gv = 1.0;
+        for (int k = 0; k < d; ++k) gv *= (k == gg) ? DL[k][ai[k]] : L[k][ai[k]];
+        dr[gg] = gv;
+      }
+      phi[i * npts + q] = v;
+      for (int k = 0; k < d; ++k) {
+        double sg = 0.0;
+        for (int gg = 0; gg < d; ++gg) sg += Ji[gg][k] * dr[gg];
+        gphys[((size_t)i * npts + q) * d + k] = sg;
+      }
+    }
+  }
+}
+
+// One boundary cell side: thermal boundaryResidual (thermal.cpp:209-260) and the same scatter as the
+// volume terms.  Neumann: res_i += -g w phi_i.  Weak Dirichlet (Nitsche, epen = 10, form_param = 1):
+// res_i += epen/h kappa (T - g) w phi_i - kappa (grad T . n) w phi_i - kappa (T - g) w (grad phi_i . n),
+// h = (sum of the side weights)^(1/(dim-1)) (workset.cpp:2719-2733).
+template <class EvalT, int N>
+void boundary_cell(const orc_problem* P, int64_t c, int face, int64_t k, const std::vector<double>& xi,
+                   const std::vector<double>& wr, const double* u, double* r, double* Jv, bool jac, bool atomic) {
+  const int d = P->dim, npe = P->npe, npts = (int)wr.size();
+  std::vector<double> x((size_t)npts * d), phi((size_t)npe * npts), gphys((size_t)npe * npts * d), w(npts),
+      nrm((size_t)npts * d);
+  side_geometry(P, c, face, xi, wr, x.data(), phi.data(), gphys.data(), w.data(), nrm.data());
+  EvalT uad[N];
+  for (int i = 0; i < npe; ++i) {
+    const double uv = u[P->lids[c * npe + i]];
+    if constexpr (std::is_same<EvalT, double>::value) uad[i] = uv; else uad[i] = EvalT(uv, i);
+  }
+  const double* g = P->bc_g[face].data() + (size_t)k * npts;
+  double hs = 0.0;
+  for (int q = 0; q < npts; ++q) hs += w[q];
+  const double h = (d == 2) ? hs : std::pow(hs, 1.0 / (d - 1.0));
+  const double epen = 10.0, sf = 1.0;
+  EvalT res[N];
+  for (int i = 0; i < npe; ++i) res[i] = EvalT(0.0);
+  for (int q = 0; q < npts; ++q) {
+    if (P->bc_kind[face] == 1) {
+      for (int i = 0; i < npe; ++i) res[i] += EvalT(-g[q] * w[q] * phi[i * npts + q]);
+      continue;
+    }
+    EvalT T = uad[0] * phi[0 * npts + q], dTn = EvalT(0.0);
+    for (int i = 1; i < npe; ++i) T += uad[i] * phi[i * npts + q];
+    for (int i = 0; i < npe; ++i) {
+      double gn = 0.0;
+      for (int m = 0; m < d; ++m) gn += gphys[((size_t)i * npts + q) * d + m] * nrm[q * d + m];
+      dTn += uad[i] * gn;
+    }
+    const EvalT diff = (P->kind == 0) ? EvalT(P->kappa[c]) : EvalT(1.0) + T * T;
+    const EvalT jump = T - EvalT(g[q]);
+    for (int i = 0; i < npe; ++i) {
+      double gin = 0.0;
+      for (int m = 0; m < d; ++m) gin += gphys[((size_t)i * npts + q) * d + m] * nrm[q * d + m];
+      res[i] += (epen / h) * diff * jump * (w[q] * phi[i * npts + q]);
+      res[i] += (-1.0) * diff * dTn * (w[q] * phi[i * npts + q]);
+      res[i] += (-sf) * diff * jump * (w[q] * gin);
+    }
+  }
+  for (int i = 0; i < npe; ++i) {
+    const int32_t row = P->lids[c * npe + i];
+    if (P->fixed[row]) continue;
+    if (r) atomic_add(&r[row], -val(res[i]), atomic);
+    if constexpr (!std::is_same<EvalT, double>::value) {
+      if (jac)
+        for (int j = 0; j < npe; ++j) atomic_add(&Jv[find_slot(P, row, P->lids[c * npe + j])], res[i].d[j], atomic);
+    }
+  }
+}
+
+template <int N>
+void assemble_boundary(orc_problem* P, const double* u, double* r, double* Jv, bool jac, int nthreads) {
+  const bool atomic = nthreads > 1;
+  for (int face = 0; face < 2 * P->dim; ++face) {
+    if (!P->bc_kind[face]) continue;
+    std::vector<double> xi, wr;
+    side_rule(P, face, xi, wr);
+    const std::vector<int64_t> cells = face_cells(P, face);
+    const int64_t nfc = (int64_t)cells.size();
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) if (nthreads > 1) schedule(static)
+#endif
+    for (int64_t k = 0; k < nfc; ++k) {
+      if (jac) boundary_cell<Dual<N>, N>(P, cells[k], face, k, xi, wr, u, r, Jv, true, atomic);
+      else boundary_cell<double, N>(P, cells[k], face, k, xi, wr, u, r, Jv, false, atomic);
+    }
+  }
+}
+
 template <int N>
 void assemble_all(orc_problem* P, const double* u, double* r, double* Jv, int flags, int nthreads) {
   bool jac = (flags & 2) && Jv;
@@ -397,6 +619,8 @@ void assemble_all(orc_problem* P, const double* u, double* r, double* Jv, int fl
       }
     }
   }
+  // boundary workset loop (jacres:485-603)
+  assemble_boundary<N>(P, u, r, Jv, jac, nthreads);
   // dofConstraints -> setJacobianConstraints: J(d,d) = 1 (constraints.hpp:125-138)
   if (jac) {
     for (int32_t dd : P->fixed_list) Jv[find_slot(P, dd, dd)] = 1.0;
@@ -505,7 +729,8 @@ orc_problem* orc_create(const orc_desc* D) {
     }
   }
   // tables
-  build_tables(P, D->quad_order > 0 ? D->quad_order : 2 * P->p);
+  P->qorder = D->quad_order > 0 ? D->quad_order : 2 * P->p;
+  build_tables(P, P->qorder);
   // Dirichlet DOFs: nodes on the selected faces, in increasing DOF order
   P->fixed.assign(P->ndof, 0);
   P->fixed_vals.assign(P->ndof, 0.0);
@@ -809,6 +1034,37 @@ void orc_tables(const orc_problem* P, double* qw, double* phi, double* dphi) {
   if (qw) std::memcpy(qw, P->qw.data(), sizeof(double) * P->nq);
   if (phi) std::memcpy(phi, P->phi.data(), sizeof(double) * P->npe * P->nq);
   if (dphi) std::memcpy(dphi, P->dphi.data(), sizeof(double) * P->npe * P->nq * P->dim);
+}
+
+// Side points of one face (face order, see side_rule / face_cells): returns the count; fills xyz
+// [count][3] (z = 0 in 2-D) when xyz is not null.  -1 for a bad face.
+int64_t orc_side_points(const orc_problem* P, int face, double* xyz) {
+  if (face < 0 || face >= 2 * P->dim) return -1;
+  std::vector<double> xi, wr;
+  side_rule(P, face, xi, wr);
+  const std::vector<int64_t> cells = face_cells(P, face);
+  const int npts = (int)wr.size(), d = P->dim;
+  if (xyz) {
+    std::vector<double> x((size_t)npts * d), phi((size_t)P->npe * npts), gp((size_t)P->npe * npts * d), w(npts),
+        nrm((size_t)npts * d);
+    for (size_t k = 0; k < cells.size(); ++k) {
+      side_geometry(P, cells[k], face, xi, wr, x.data(), phi.data(), gp.data(), w.data(), nrm.data());
+      for (int q = 0; q < npts; ++q)
+        for (int m = 0; m < 3; ++m) xyz[((k * npts) + q) * 3 + m] = (m < d) ? x[q * d + m] : 0.0;
+    }
+  }
+  return (int64_t)cells.size() * npts;
+}
+
+// Boundary condition of one face: kind 0 none, 1 Neumann, 2 weak Dirichlet; g has one value per side
+// point (orc_side_points order), null means zero.  Returns 0, or -1 on bad input.
+int orc_set_face_bc(orc_problem* P, int face, int kind, const double* g) {
+  if (face < 0 || face >= 2 * P->dim || kind < 0 || kind > 2) return -1;
+  const int64_t n = orc_side_points(P, face, nullptr);
+  P->bc_kind[face] = kind;
+  P->bc_g[face].assign(n, 0.0);
+  if (g) for (int64_t i = 0; i < n; ++i) P->bc_g[face][i] = g[i];
+  return 0;
 }
 
 int orc_max_threads(void) {

@@ -69,6 +69,10 @@ def lib():
         L.orc_errors.argtypes = [P, dp, C.c_double, C.c_double, dp, dp]
         L.orc_tables.argtypes = [P, dp, dp, dp]
         L.orc_max_threads.restype = C.c_int
+        L.orc_side_points.argtypes = [P, C.c_int, dp]
+        L.orc_side_points.restype = C.c_int64
+        L.orc_set_face_bc.argtypes = [P, C.c_int, C.c_int, dp]
+        L.orc_set_face_bc.restype = C.c_int
         _lib = L
     return _lib
 
@@ -187,6 +191,21 @@ class OracleProblem:
         st = np.zeros(3)
         rc = lib().orc_newton(self.h, _dp(u), nltol, maxiter, lintol, linmaxiter, nthreads, _dp(st))
         return u, rc, st
+
+    def side_points(self, face):
+        """Coordinates [npts, 3] of the side quadrature points of `face` (face-cell order)."""
+        n = lib().orc_side_points(self.h, int(face), None)
+        if n < 0:
+            raise ValueError(f"bad face {face}")
+        xyz = np.zeros((n, 3))
+        lib().orc_side_points(self.h, int(face), _dp(xyz))
+        return xyz
+
+    def set_face_bc(self, face, kind, g=None):
+        """kind: 0 none, 1 Neumann, 2 weak Dirichlet; g: one value per side point (None = 0)."""
+        ga = None if g is None else np.ascontiguousarray(g, dtype=np.float64)
+        if lib().orc_set_face_bc(self.h, int(face), int(kind), None if ga is None else _dp(ga)) != 0:
+            raise ValueError("bad face boundary condition")
 
     def errors(self, u, amp, freq):
         l2 = np.zeros(1)

@@ -25,6 +25,10 @@ CASES = {
                                        dirichlet=["sinprod_l2", 1.0, 1.0], exact=["1", "1"]),
     "3D-Multiblock": dict(dim=3, order=1, n=[10, 10, 10], quad_order=2, source=["sinprod", "12*pi^2", "2*pi"],
                           dirichlet=["const", 0.0], exact=["1", "2*pi"], workset_size=1),
+    # strong Dirichlet on left/right only (faces x-, x+), Neumann data on bottom (y-) / top (y+)
+    "2D_mixed_bcs": dict(dim=2, order=1, n=[40, 40], quad_order=2, source=["sinprod", "8*pi^2", "2*pi"],
+                         dirichlet=["const", 0.0], dirichlet_faces=3, exact=["1", "2*pi"],
+                         neumann=[[2, "-2*pi*sin(2*pi*x)*cos(2*pi*y)"], [3, "2*pi*sin(2*pi*x)*cos(2*pi*y)"]]),
 }
 
 
