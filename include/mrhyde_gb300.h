@@ -185,8 +185,9 @@ typedef struct mrg_solve_stats {
   int32_t reserved;
 } mrg_solve_stats;
 
-/* Jacobi PCG on J x = b (x holds the initial guess).  Same iteration and stopping test as the
-   reference (rel. 2-norm).  Synchronises `stream` once at the end to return stats. */
+/* PCG on J x = b (x holds the initial guess).  Same iteration and stopping test as the reference
+   (rel. 2-norm); Jacobi preconditioning unless mrg_set_preconditioner chose multigrid.  Synchronises
+   `stream` once at the end to return stats. */
 int mrg_solve_pcg(mrg_problem* p, const void* J_vals_dev, int32_t J_fp32, const double* b_dev, double* x_dev,
                   double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
 
@@ -198,6 +199,16 @@ int mrg_solve_bicgstab(mrg_problem* p, const void* J_vals_dev, int32_t J_fp32, c
                        double rtol, int32_t maxiter, mrg_solve_stats* stats, mrg_stream_t stream);
 
 enum { MRG_KRYLOV_AUTO = 0, MRG_KRYLOV_PCG = 1, MRG_KRYLOV_BICGSTAB = 2 };
+
+/* Preconditioner of the CG used by mrg_solve_pcg and by mrg_newton's CG branch.
+     MRG_PREC_JACOBI  diagonal scaling: the reference's SolverManager::PCG (default)
+     MRG_PREC_GMG     geometric multigrid V(2,2)-cycle on the structured grid: Galerkin coarse operators,
+                      Chebyshev-Jacobi smoothing, dense coarsest solve -- the structured-grid counterpart
+                      of the reference's MueLu multigrid option for Belos
+                      (src/interfaces/linear_algebra/linearAlgebraInterface_solvers.hpp:15-160).
+                      Q1 problems only (MRG_ENOTSUP for Q2).  Runs in the precision of the Jacobian. */
+enum { MRG_PREC_JACOBI = 0, MRG_PREC_GMG = 1 };
+int mrg_set_preconditioner(mrg_problem* p, int32_t kind);
 
 typedef struct mrg_newton_opts {
   double nl_tol;        /* relative inf-norm tolerance ("nonlinear TOL")                       */

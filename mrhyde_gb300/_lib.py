@@ -62,6 +62,7 @@ class SolveStats(C.Structure):
 
 
 MRG_KRYLOV_AUTO, MRG_KRYLOV_PCG, MRG_KRYLOV_BICGSTAB = 0, 1, 2
+MRG_PREC_JACOBI, MRG_PREC_GMG = 0, 1
 
 
 class NewtonOpts(C.Structure):
@@ -103,6 +104,7 @@ SIGNATURES = {
     "mrg_set_dirichlet": (C.c_int, [_VP, _VP, _VP]),
     "mrg_get_side_points": (C.c_int, [_VP, C.c_int32, C.POINTER(C.c_int64), _VP]),
     "mrg_set_face_bc": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP]),
+    "mrg_set_preconditioner": (C.c_int, [_VP, C.c_int32]),
     "mrg_assemble": (C.c_int, [_VP, _VP, _VP, _VP, C.c_uint32, _VP]),
     "mrg_spmv": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "mrg_solve_pcg": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),

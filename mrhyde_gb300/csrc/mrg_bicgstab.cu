@@ -330,6 +330,11 @@ int mrg_bicg_solve64(mrg_problem* p, const double* J, const double* b, double* x
   return bicg_run<double, double>(p, J, b, x, false, rtol, maxiter, st, s);
 }
 
+__global__ void k_b_add(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += d[i];
+}
+
 __global__ void k_b_addf(int64_t n, const float* __restrict__ d, double* __restrict__ x) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] += (double)d[i];
@@ -341,6 +346,24 @@ extern "C" int mrg_solve_bicgstab(mrg_problem* p, const void* J, int32_t fp32, c
   if (!(rtol >= 0.0) || maxiter < 0) return mrg_fail(MRG_EINVAL, "mrg_solve_bicgstab: bad tolerance or iteration limit");
   cudaStream_t s = (cudaStream_t)stream;
   p->last_stream = s;
+  if (mrg_gmg_kind(p) == MRG_PREC_GMG) {
+    // multigrid-preconditioned BiCGStab on the correction: J dx = b - J x, x += dx
+    double *res = nullptr, *dx = nullptr;
+    MRG_CUDA(cudaMallocAsync(&res, p->ndof * sizeof(double), s));
+    MRG_CUDA(cudaMallocAsync(&dx, p->ndof * sizeof(double), s));
+    int rc = mrg_spmv(p, J, fp32, x, res, stream);
+    if (rc == MRG_OK) rc = mrg_residual_from(p, b, res, s);
+    if (rc == MRG_OK) rc = mrg_gmg_bicgstab(p, J, fp32 != 0, res, dx, rtol, maxiter, st, s);
+    if (rc == MRG_OK || rc == MRG_ENOCONV) {
+      k_b_add<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, dx, x);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess && rc == MRG_OK) rc = mrg_cuda_check(e, "BiCGStab update");
+    }
+    cudaFreeAsync(res, s);
+    cudaFreeAsync(dx, s);
+    cudaStreamSynchronize(s);
+    return rc;
+  }
   if (!fp32) return mrg_bicg_solve64(p, (const double*)J, b, x, rtol, maxiter, st, s);
   // FP32 matrix: the correction of x from J32 d = b - J32 x (residual formed in FP64 by the SpMV)
   double* res = nullptr;

@@ -1,0 +1,1105 @@
+// Geometric multigrid preconditioner for Q1 problems on the structured graph, and the CG that uses it.
+//
+// The reference's linear solver is Belos with an algebraic multigrid preconditioner (MueLu) or its own
+// Jacobi PCG (src/managers/solver/solverManager_solvers.hpp:812-901; Belos/MueLu options in
+// src/interfaces/linear_algebra/linearAlgebraInterface_solvers.hpp:15-160).  On the structured box the
+// multigrid hierarchy is known in closed form, so it is built geometrically and Galerkin-exactly:
+//
+//   * levels: vertex coarsening by 2 along the axes that still have >= 3 cells and whose cells are at
+//     most twice as long as the shortest (semi-coarsening on stretched grids); a fine node with an
+//     even index is a coarse node, and when the cell count is odd the last fine node is kept as a coarse
+//     node too (the last coarse cell is one fine cell wide).  Every level has the canonical 27-point
+//     (9-point in 2-D) layout of a p = 1 grid, so the level operators use the same CSR layout, row
+//     formulas and staged SpMV as the fine one.
+//   * interpolation P: tensor product of 1-D linear interpolation (weights 1 or 1/2); rows of fixed
+//     (strong Dirichlet) fine nodes and columns of fixed coarse nodes are zero, so the hierarchy acts on
+//     the free unknowns only, where J is symmetric.
+//   * coarse operators A_c = P^T A_f P (restricted to free nodes; fixed coarse rows are identity rows),
+//     computed as one 1-D Galerkin sweep per coarsened axis (the masked P is a tensor product).
+//   * smoother: Chebyshev polynomial of degree 2 in D^{-1} A on [0.25 L, L], L the Gershgorin bound
+//     max_i sum_j |a_ij| / a_ii of the level (computed on the device; no host synchronisation);
+//   * coarsest level (at most 27 unknowns): dense inverse, Gauss-Jordan on the device.
+//   * V(2,2) cycle, symmetric, so it preconditions CG.
+//
+// The CG keeps q = A p by recurrence (p <- z + beta p, q <- A z + beta q) so the SpMV reads z and no
+// separate direction update is needed; dot products reduce deterministically (per-block partials,
+// last block sums in index order).  The hierarchy and the CG run in the precision of the Jacobian
+// (FP64, or FP32 for the inner solve of the mixed path).  Chunks of iterations are captured as CUDA
+// graphs; the host reads the done flag once per chunk.
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mrg_device.cuh"
+#include "mrg_internal.h"
+
+namespace {
+
+using namespace mrgdev;
+
+constexpr int NT = WST;            // threads per CTA
+constexpr int NU = 2;              // Chebyshev degree (pre and post smoothing)
+constexpr double CHEB_LO = 0.25;   // lower end of the smoothed interval, fraction of the bound
+constexpr int GCHUNK = 4;          // CG iterations per captured graph
+constexpr int MAXC = 32;           // largest coarsest level solved densely
+constexpr int MAXLEV = 16;
+
+// ---- 1-D transfer along one axis ----------------------------------------------------------------
+// Parents of fine node i (fine nodes 0..nnf-1, coarse nodes 0..nnc-1) with interpolation weights.
+__host__ __device__ inline int axis_parents(int i, int nnf, int nnc, int coarsen, int* pc, float* pw) {
+  if (!coarsen) { pc[0] = i; pw[0] = 1.0f; return 1; }
+  if ((i & 1) == 0) { pc[0] = i >> 1; pw[0] = 1.0f; return 1; }
+  if (i == nnf - 1) { pc[0] = nnc - 1; pw[0] = 1.0f; return 1; }  // odd last node is kept
+  pc[0] = (i - 1) >> 1; pw[0] = 0.5f;
+  pc[1] = (i + 1) >> 1; pw[1] = 0.5f;
+  return 2;
+}
+
+// Children of coarse node c with their weights (the transpose of axis_parents).
+__device__ inline int axis_children(int c, int nnf, int nnc, int coarsen, int* ci, float* cw) {
+  if (!coarsen) { ci[0] = c; cw[0] = 1.0f; return 1; }
+  int n = 0;
+  for (int i = 2 * c - 1; i <= 2 * c + 1; ++i) {
+    if (i < 0 || i >= nnf) continue;
+    int pc[2];
+    float pw[2];
+    const int np = axis_parents(i, nnf, nnc, 1, pc, pw);
+    for (int k = 0; k < np; ++k)
+      if (pc[k] == c) { ci[n] = i; cw[n] = pw[k]; ++n; }
+  }
+  return n;
+}
+
+struct Xfer {
+  int co[3];  // axis coarsened from the finer level
+};
+
+template <typename T>
+struct LevDev {
+  Grid g;
+  int64_t n;
+  const T* A;
+  T* minv;
+  T *xa, *xb, *d, *b, *r;
+};
+
+struct GScal {
+  double rho, pq, alpha, beta, r0, rnorm, tol;
+  double omega, rv;  // BiCGStab
+  int iter, maxiter, done, status;
+  unsigned int counter;
+  int err;
+};
+
+template <typename T>
+__device__ __forceinline__ auto row_prod(const Grid& g, const RowInfo& R, const T* vals, const T* x) {
+  if constexpr (sizeof(T) == 4) return row_apply_f<1>(g, R, vals, x);
+  else return row_apply<1, double, double>(g, R, vals, x);
+}
+
+__device__ __forceinline__ bool is_done(const GScal* S) { return ((volatile const GScal*)S)->done != 0; }
+
+// ---- setup kernels ------------------------------------------------------------------------------
+// One axis of the Galerkin product, one thread per row of the output grid gc (gc = gf coarsened along
+// `axis` only).  The free nodes form a Cartesian product (Dirichlet faces are axis-aligned), so the
+// masked interpolation is a tensor product and P^T A P is three such sweeps (x, then y, then z),
+// each keeping the 27-point layout on an intermediate grid: ~160 multiply-adds per output row instead
+// of ~5,800 for the direct triple product.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, Grid gc, int axis, const T* __restrict__ Af,
+                                                 T* __restrict__ Ac, int* __restrict__ err) {
+  const int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x;
+  const int64_t nrows = (int64_t)gc.nn[0] * gc.nn[1] * gc.nn[2];
+  if (n >= nrows) return;
+  int I[3];
+  decompose(gc, n, I[0], I[1], I[2]);
+  const RowInfo Rc = row_info<1>(gc, I[0], I[1], I[2]);
+  const int lenc = Rc.cx * Rc.cy * Rc.cz;
+  T* out = Ac + Rc.rp;
+  if (node_fixed(gc, I[0], I[1], I[2])) {
+    const int dg = (int)(diag_pos(Rc, I[0], I[1], I[2]) - Rc.rp);
+    for (int e = 0; e < lenc; ++e) out[e] = (e == dg) ? T(1) : T(0);
+    return;
+  }
+  T acc[27];
+#pragma unroll
+  for (int e = 0; e < 27; ++e) acc[e] = T(0);
+  int ci[3];
+  float cw[3];
+  const int nci = axis_children(I[axis], gf.nn[axis], gc.nn[axis], 1, ci, cw);
+  for (int c = 0; c < nci; ++c) {
+    int f[3] = {I[0], I[1], I[2]};
+    f[axis] = ci[c];
+    if (node_fixed(gf, f[0], f[1], f[2])) continue;
+    const RowInfo Rf = row_info<1>(gf, f[0], f[1], f[2]);
+    const T* vals = Af + Rf.rp;
+    int e = 0;
+    for (int jz = Rf.lz; jz < Rf.lz + Rf.cz; ++jz)
+      for (int jy = Rf.ly; jy < Rf.ly + Rf.cy; ++jy)
+        for (int jx = Rf.lx; jx < Rf.lx + Rf.cx; ++jx, ++e) {
+          if (node_fixed(gf, jx, jy, jz)) continue;
+          const T a = vals[e] * (T)cw[c];
+          int jj[3] = {jx, jy, jz};
+          int pc[2];
+          float pw[2];
+          const int np = axis_parents(jj[axis], gf.nn[axis], gc.nn[axis], 1, pc, pw);
+          for (int k = 0; k < np; ++k) {
+            jj[axis] = pc[k];
+            if (node_fixed(gc, jj[0], jj[1], jj[2])) continue;
+            const int pos = ((jj[2] - Rc.lz) * Rc.cy + (jj[1] - Rc.ly)) * Rc.cx + (jj[0] - Rc.lx);
+            if (pos < 0 || pos >= lenc) { atomicExch(err, 1); continue; }
+            acc[pos] += a * (T)pw[k];
+          }
+        }
+  }
+  for (int e = 0; e < lenc; ++e) out[e] = acc[e];
+}
+
+// minv = 1 / diag; Gershgorin bound max_i sum_j |a_ij| / |a_ii| into lmax (as float bits, atomicMax)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_diag(Grid g, const T* __restrict__ A, T* __restrict__ minv,
+                                             unsigned int* __restrict__ lmax_bits) {
+  const int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x;
+  const int64_t nrows = (int64_t)g.nn[0] * g.nn[1] * g.nn[2];
+  float v = 0.0f;
+  if (n < nrows) {
+    int ix, iy, iz;
+    decompose(g, n, ix, iy, iz);
+    const RowInfo R = row_info<1>(g, ix, iy, iz);
+    const T* vals = A + R.rp;
+    const int len = R.cx * R.cy * R.cz;
+    const T dgv = vals[diag_pos(R, ix, iy, iz) - R.rp];
+    double s = 0.0;
+    for (int e = 0; e < len; ++e) s += fabs((double)vals[e]);
+    minv[n] = T(1) / dgv;
+    v = (float)(s / fabs((double)dgv));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v > 0.0f) atomicMax(lmax_bits, __float_as_uint(v));
+}
+
+// Dense inverse of the coarsest operator (n <= MAXC), Gauss-Jordan with partial pivoting, one CTA.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_coarse_inv(Grid g, const T* __restrict__ A, T* __restrict__ inv,
+                                                   int* __restrict__ err) {
+  __shared__ double M[MAXC][2 * MAXC];
+  __shared__ int piv;
+  const int n = g.nn[0] * g.nn[1] * g.nn[2];
+  for (int k = threadIdx.x; k < MAXC * 2 * MAXC; k += NT) (&M[0][0])[k] = 0.0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += NT) {
+    int ix, iy, iz;
+    decompose(g, i, ix, iy, iz);
+    const RowInfo R = row_info<1>(g, ix, iy, iz);
+    int e = 0;
+    for (int jz = R.lz; jz < R.lz + R.cz; ++jz)
+      for (int jy = R.ly; jy < R.ly + R.cy; ++jy)
+        for (int jx = R.lx; jx < R.lx + R.cx; ++jx, ++e)
+          M[i][jx + g.nn[0] * (jy + g.nn[1] * jz)] = (double)A[R.rp + e];
+    M[i][n + i] = 1.0;
+  }
+  __syncthreads();
+  for (int c = 0; c < n; ++c) {
+    if (threadIdx.x == 0) {
+      int best = c;
+      for (int r = c + 1; r < n; ++r)
+        if (fabs(M[r][c]) > fabs(M[best][c])) best = r;
+      piv = best;
+      if (!(fabs(M[best][c]) > 0.0)) atomicExch(err, 2);
+    }
+    __syncthreads();
+    const int pr = piv;
+    if (pr != c)
+      for (int k = threadIdx.x; k < 2 * n; k += NT) {
+        const double t = M[c][k];
+        M[c][k] = M[pr][k];
+        M[pr][k] = t;
+      }
+    __syncthreads();
+    const double inv_p = 1.0 / M[c][c];
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * n; k += NT) M[c][k] *= inv_p;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * 2 * n; idx += NT) {
+      const int r = idx / (2 * n), k = idx % (2 * n);
+      if (r != c && k != c) M[r][k] -= M[r][c] * M[c][k];
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += NT)
+      if (r != c) M[r][c] = 0.0;
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < n * n; idx += NT) inv[idx] = (T)M[idx / n][n + idx % n];
+}
+
+// ---- cycle kernels --------------------------------------------------------------------------------
+// Chebyshev step `k` (0..NU-1): d = rho_k rho_{k-1} d + (2 rho_k / delta) D^{-1}(b - A x)  (k = 0:
+// d = D^{-1}(b - A x) / theta); xout = x + d.  zero_x: x = 0 (no SpMV).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_cheb(LevDev<T> L, const T* __restrict__ xin, T* __restrict__ xout, int k,
+                                             int zero_x, const unsigned int* __restrict__ lmax_bits,
+                                             const GScal* __restrict__ S, int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
+  if (is_done(S)) return;
+  const double hi = (double)__uint_as_float(*lmax_bits), lo = CHEB_LO * hi;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  double rho_prev = 1.0 / sigma, rho = rho_prev;
+  for (int j = 1; j <= k; ++j) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    rho_prev = rho;
+    rho = rn;
+  }
+  const T c_old = (T)(rho * rho_prev), c_new = (T)(2.0 * rho / delta), c_first = (T)(1.0 / theta);
+  auto fin = [&](int64_t n, T ax) {
+    const T z = L.minv[n] * (L.b[n] - ax);
+    const T d = (k == 0) ? c_first * z : c_old * L.d[n] + c_new * z;
+    L.d[n] = d;
+    xout[n] = (zero_x ? T(0) : xin[n]) + d;
+  };
+  if (zero_x) {
+    for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < L.n; n += (int64_t)gridDim.x * NT) fin(n, T(0));
+    return;
+  }
+  const bool ok = warp_staged_rows<T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
+    fin(n, (T)row_prod<T>(L.g, R, vals, xin));
+  });
+  if (!ok) atomicExch(err, 3);
+}
+
+// r = b - A x
+template <typename T>
+__global__ void __launch_bounds__(NT) k_resid(LevDev<T> L, const T* __restrict__ x, const GScal* __restrict__ S,
+                                              int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
+  if (is_done(S)) return;
+  const bool ok = warp_staged_rows<T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
+    L.r[n] = L.b[n] - (T)row_prod<T>(L.g, R, vals, x);
+  });
+  if (!ok) atomicExch(err, 3);
+}
+
+// b_c = P^T r_f
+template <typename T>
+__global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const T* __restrict__ rf, T* __restrict__ bc,
+                                                 const GScal* __restrict__ S) {
+  if (is_done(S)) return;
+  const int64_t nc = (int64_t)gc.nn[0] * gc.nn[1] * gc.nn[2];
+  for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < nc; n += (int64_t)gridDim.x * NT) {
+    int I[3];
+    decompose(gc, n, I[0], I[1], I[2]);
+    if (node_fixed(gc, I[0], I[1], I[2])) { bc[n] = T(0); continue; }
+    int ci[3][3];
+    float cw[3][3];
+    int nci[3];
+    for (int k = 0; k < 3; ++k) {
+      if (k < gf.dim) nci[k] = axis_children(I[k], gf.nn[k], gc.nn[k], X.co[k], ci[k], cw[k]);
+      else { nci[k] = 1; ci[k][0] = 0; cw[k][0] = 1.0f; }
+    }
+    T s = T(0);
+    for (int a2 = 0; a2 < nci[2]; ++a2)
+      for (int a1 = 0; a1 < nci[1]; ++a1)
+        for (int a0 = 0; a0 < nci[0]; ++a0) {
+          const int ix = ci[0][a0], iy = ci[1][a1], iz = ci[2][a2];
+          if (node_fixed(gf, ix, iy, iz)) continue;
+          s += (T)(cw[0][a0] * cw[1][a1] * cw[2][a2]) * rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)];
+        }
+    bc[n] = s;
+  }
+}
+
+// x_f += P x_c
+template <typename T>
+__global__ void __launch_bounds__(NT) k_prolong(Grid gf, Grid gc, Xfer X, const T* __restrict__ xc, T* __restrict__ xf,
+                                                const GScal* __restrict__ S) {
+  if (is_done(S)) return;
+  const int64_t nf = (int64_t)gf.nn[0] * gf.nn[1] * gf.nn[2];
+  for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < nf; n += (int64_t)gridDim.x * NT) {
+    int i[3];
+    decompose(gf, n, i[0], i[1], i[2]);
+    if (node_fixed(gf, i[0], i[1], i[2])) continue;
+    int pc[3][2];
+    float pw[3][2];
+    int np[3];
+    for (int k = 0; k < 3; ++k) {
+      if (k < gf.dim) np[k] = axis_parents(i[k], gf.nn[k], gc.nn[k], X.co[k], pc[k], pw[k]);
+      else { np[k] = 1; pc[k][0] = 0; pw[k][0] = 1.0f; }
+    }
+    T s = T(0);
+    for (int b2 = 0; b2 < np[2]; ++b2)
+      for (int b1 = 0; b1 < np[1]; ++b1)
+        for (int b0 = 0; b0 < np[0]; ++b0) {
+          if (node_fixed(gc, pc[0][b0], pc[1][b1], pc[2][b2])) continue;
+          s += (T)(pw[0][b0] * pw[1][b1] * pw[2][b2]) *
+               xc[pc[0][b0] + (int64_t)gc.nn[0] * (pc[1][b1] + (int64_t)gc.nn[1] * pc[2][b2])];
+        }
+    xf[n] += s;
+  }
+}
+
+// x = inv b on the coarsest level
+template <typename T>
+__global__ void __launch_bounds__(NT) k_coarse_apply(int n, const T* __restrict__ inv, const T* __restrict__ b,
+                                                     T* __restrict__ x, const GScal* __restrict__ S) {
+  if (is_done(S)) return;
+  for (int i = threadIdx.x; i < n; i += NT) {
+    T s = T(0);
+    for (int j = 0; j < n; ++j) s += inv[i * n + j] * b[j];
+    x[i] = s;
+  }
+}
+
+// ---- CG kernels -----------------------------------------------------------------------------------
+template <typename T>
+struct CgVec {
+  T *x, *r, *p, *q;
+  const T* z;
+  double* parts;
+  GScal* S;
+};
+
+// x = 0, r = b (FP64 in, T out), p = q = 0; r0 = |r|
+template <typename T>
+__global__ void __launch_bounds__(NT) k_cg_init(int64_t n, const double* __restrict__ b, CgVec<T> V) {
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+    const T r = (T)b[i];
+    V.x[i] = T(0);
+    V.r[i] = r;
+    V.p[i] = T(0);
+    V.q[i] = T(0);
+    rr += (double)r * (double)r;
+  }
+  double m[1] = {block_sum(rr)};
+  if (last_block<1>(V.parts, m, &V.S->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      S->r0 = sqrt(t[0]);
+      S->rnorm = S->r0;
+      S->iter = 0;
+      S->status = MRG_OK;
+      S->beta = 0.0;
+      S->rho = 0.0;
+      S->done = (S->r0 == 0.0 || S->maxiter <= 0) ? 1 : 0;
+      if (!isfinite(S->r0)) { S->done = 1; S->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+// rho_new = r . z ; beta = rho_new / rho (0 on the first call)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_cg_rz(int64_t n, CgVec<T> V, int first) {
+  if (is_done(V.S)) return;
+  double rz = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
+    rz += (double)V.r[i] * (double)V.z[i];
+  double m[1] = {block_sum(rz)};
+  if (last_block<1>(V.parts, m, &V.S->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      S->beta = first ? 0.0 : t[0] / S->rho;
+      S->rho = t[0];
+      if (!(t[0] > 0.0) || !isfinite(t[0])) { S->status = MRG_ENUMERIC; S->done = 1; }
+    }
+  }
+}
+
+// w = A z ; p = z + beta p ; q = w + beta q ; partial p.q ; alpha = rho / p.q
+template <typename T>
+__global__ void __launch_bounds__(NT) k_cg_spmv(Grid g, int64_t n, const T* __restrict__ A, CgVec<T> V) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
+  if (is_done(V.S)) return;
+  const T beta = (T)V.S->beta;
+  double pq = 0.0;
+  const bool ok = warp_staged_rows<T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
+    const T w = (T)row_prod<T>(g, R, vals, V.z);
+    const T pn = V.z[i] + beta * V.p[i];
+    const T qn = w + beta * V.q[i];
+    V.p[i] = pn;
+    V.q[i] = qn;
+    pq += (double)pn * (double)qn;
+  });
+  if (!ok) atomicExch(&V.S->err, 3);
+  double m[1] = {block_sum(pq)};
+  if (last_block<1>(V.parts, m, &V.S->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      S->pq = t[0];
+      S->alpha = S->rho / t[0];
+      if (!(t[0] > 0.0) || !isfinite(S->alpha)) { S->status = MRG_ENUMERIC; S->done = 1; }
+      if (S->err) { S->status = MRG_ETIMEOUT; S->done = 1; }
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha q ; |r| ; stopping test
+template <typename T>
+__global__ void __launch_bounds__(NT) k_cg_update(int64_t n, CgVec<T> V) {
+  if (is_done(V.S)) return;
+  const T alpha = (T)V.S->alpha;
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+    V.x[i] += alpha * V.p[i];
+    const T r = V.r[i] - alpha * V.q[i];
+    V.r[i] = r;
+    rr += (double)r * (double)r;
+  }
+  double m[1] = {block_sum(rr)};
+  if (last_block<1>(V.parts, m, &V.S->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      S->rnorm = sqrt(t[0]);
+      S->iter += 1;
+      if (!(S->rnorm / S->r0 > S->tol) || S->iter >= S->maxiter) S->done = 1;
+      if (!isfinite(S->rnorm)) { S->done = 1; S->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_to_f64(int64_t n, const T* __restrict__ a, double* __restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+
+// ---- BiCGStab kernels (right preconditioning by the same V-cycle) ------------------------------
+template <typename T>
+struct BgVec {
+  T *x, *r, *rh, *p, *v, *s, *t, *ph, *sh;
+  double* parts;
+  GScal* S;
+};
+
+// x = 0, r = rh = b, p = v = 0; rho = (rh . r), alpha = omega = 1, beta = 0
+template <typename T>
+__global__ void __launch_bounds__(NT) k_bg_init(int64_t n, const double* __restrict__ b, BgVec<T> V) {
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+    const T r = (T)b[i];
+    V.x[i] = T(0);
+    V.r[i] = r;
+    V.rh[i] = r;
+    V.p[i] = T(0);
+    V.v[i] = T(0);
+    rr += (double)r * (double)r;
+  }
+  double m[1] = {block_sum(rr)};
+  if (last_block<1>(V.parts, m, &V.S->counter)) {
+    double t[1];
+    sum_parts<1>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      S->r0 = sqrt(t[0]);
+      S->rnorm = S->r0;
+      S->rho = t[0];
+      S->alpha = 1.0;
+      S->omega = 1.0;
+      S->beta = 0.0;
+      S->iter = 0;
+      S->status = MRG_OK;
+      S->done = (S->r0 == 0.0 || S->maxiter <= 0) ? 1 : 0;
+      if (!isfinite(S->r0)) { S->done = 1; S->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+// p = r + beta (p - omega v)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_bg_p(int64_t n, BgVec<T> V) {
+  if (is_done(V.S)) return;
+  const T beta = (T)V.S->beta, omega = (T)V.S->omega;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
+    V.p[i] = V.r[i] + beta * (V.p[i] - omega * V.v[i]);
+}
+
+// STEP 0: v = A ph, rv = rh . v, alpha = rho / rv.   STEP 1: t = A sh, omega = (t . s) / (t . t).
+template <typename T, int STEP>
+__global__ void __launch_bounds__(NT) k_bg_spmv(Grid g, int64_t n, const T* __restrict__ A, BgVec<T> V) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
+  if (is_done(V.S)) return;
+  const T* in = STEP == 0 ? V.ph : V.sh;
+  T* out = STEP == 0 ? V.v : V.t;
+  double d0 = 0.0, d1 = 0.0;
+  const bool ok = warp_staged_rows<T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
+    const T y = (T)row_prod<T>(g, R, vals, in);
+    out[i] = y;
+    if (STEP == 0) {
+      d0 += (double)V.rh[i] * (double)y;
+    } else {
+      d0 += (double)y * (double)V.s[i];
+      d1 += (double)y * (double)y;
+    }
+  });
+  if (!ok) atomicExch(&V.S->err, 3);
+  double m[2] = {block_sum(d0), block_sum(d1)};
+  if (last_block<2>(V.parts, m, &V.S->counter)) {
+    double t[2];
+    sum_parts<2>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      if (STEP == 0) {
+        S->rv = t[0];
+        S->alpha = S->rho / t[0];
+        if (!(t[0] != 0.0) || !isfinite(S->alpha)) { S->status = MRG_ENUMERIC; S->done = 1; }
+      } else {
+        S->omega = (t[1] > 0.0) ? t[0] / t[1] : 0.0;
+      }
+      if (S->err) { S->status = MRG_ETIMEOUT; S->done = 1; }
+    }
+  }
+}
+
+// s = r - alpha v
+template <typename T>
+__global__ void __launch_bounds__(NT) k_bg_s(int64_t n, BgVec<T> V) {
+  if (is_done(V.S)) return;
+  const T alpha = (T)V.S->alpha;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
+    V.s[i] = V.r[i] - alpha * V.v[i];
+}
+
+// x += alpha ph + omega sh ; r = s - omega t ; |r|, rh . r -> beta for the next direction; stopping test
+template <typename T>
+__global__ void __launch_bounds__(NT) k_bg_update(int64_t n, BgVec<T> V) {
+  if (is_done(V.S)) return;
+  const T alpha = (T)V.S->alpha, omega = (T)V.S->omega;
+  double rr = 0.0, rhr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+    V.x[i] += alpha * V.ph[i] + omega * V.sh[i];
+    const T r = V.s[i] - omega * V.t[i];
+    V.r[i] = r;
+    rr += (double)r * (double)r;
+    rhr += (double)V.rh[i] * (double)r;
+  }
+  double m[2] = {block_sum(rr), block_sum(rhr)};
+  if (last_block<2>(V.parts, m, &V.S->counter)) {
+    double t[2];
+    sum_parts<2>(V.parts, t, &V.S->counter);
+    if (threadIdx.x == 0) {
+      GScal* S = V.S;
+      S->rnorm = sqrt(t[0]);
+      S->iter += 1;
+      S->beta = (t[1] / S->rho) * (S->alpha / S->omega);
+      S->rho = t[1];
+      if (!(S->rnorm / S->r0 > S->tol) || S->iter >= S->maxiter) S->done = 1;
+      if (!isfinite(S->rnorm)) { S->done = 1; S->status = MRG_ENUMERIC; }
+      else if (!S->done && (!(t[1] != 0.0) || !(S->omega != 0.0))) { S->done = 1; S->status = MRG_ENUMERIC; }
+    }
+  }
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int num_sms() {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
+  }
+  return nsm;
+}
+
+unsigned grid_for(int64_t n, int per_sm) {
+  const unsigned need = nblk(n, NT), cap = (unsigned)(per_sm * num_sms());
+  return need < cap ? need : cap;
+}
+
+template <typename T>
+constexpr int staged_per_sm() { return sizeof(T) == 8 ? 4 : 7; }
+
+// ---- hierarchy ------------------------------------------------------------------------------------
+struct HLevel {
+  Grid g;
+  int64_t n = 0, nnz = 0;
+  Xfer X{{0, 0, 0}};          // how this level was coarsened from the finer one
+  int nsweep = 0;             // Galerkin sweeps from the finer level (one per coarsened axis)
+  int sweep_axis[3] = {0, 0, 0};
+  Grid mid[2];                // intermediate grids after all but the last sweep
+  int64_t* d_mid_pref[2] = {nullptr, nullptr};
+  int64_t* d_pref = nullptr;  // prefix tables (coarse levels)
+  void* A = nullptr;          // coarse levels: owned; level 0: the caller's Jacobian
+  void *minv = nullptr, *xa = nullptr, *xb = nullptr, *d = nullptr, *b = nullptr, *r = nullptr;
+};
+
+template <typename T>
+struct Hier {
+  std::vector<HLevel> L;
+  T* cinv = nullptr;
+  T* mid[2] = {nullptr, nullptr};  // intermediate operators of the Galerkin sweeps
+  unsigned int* lmax = nullptr;   // [nlev] float bits
+  int* err = nullptr;             // setup / cycle error word
+  T *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr;  // CG vectors (level-0 size)
+  double* parts = nullptr;
+  GScal* S = nullptr;
+  GScal* h_S = nullptr;           // pinned mirror
+  cudaGraphExec_t graph = nullptr;
+  const void* graph_A = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  // BiCGStab vectors (allocated on first use) and its captured chunk
+  T *rh = nullptr, *v = nullptr, *sv = nullptr, *t = nullptr, *ph = nullptr, *sh = nullptr;
+  cudaGraphExec_t bgraph = nullptr;
+  const void* bgraph_A = nullptr;
+  cudaStream_t bgraph_stream = nullptr;
+};
+
+struct GmgData {
+  int kind = MRG_PREC_JACOBI;
+  Hier<double>* h64 = nullptr;
+  Hier<float>* h32 = nullptr;
+};
+
+GmgData* gdata(mrg_problem* p) {
+  if (!p->gmg) p->gmg = new GmgData();
+  return reinterpret_cast<GmgData*>(p->gmg);
+}
+
+// Host grid of a p = 1 level with nn nodes per axis (prefix tables uploaded to d_pref).
+int make_level_grid(const Grid& fine, const int nn[3], cudaStream_t s, Grid& g, int64_t*& d_pref) {
+  g = fine;
+  g.p = 1;
+  for (int k = 0; k < 3; ++k) {
+    g.nn[k] = nn[k];
+    g.nc[k] = (k < fine.dim) ? nn[k] - 1 : 1;
+  }
+  std::vector<int64_t> pref;
+  int64_t offs[3];
+  for (int k = 0; k < 3; ++k) {
+    offs[k] = (int64_t)pref.size();
+    int64_t acc = 0;
+    pref.push_back(0);
+    for (int i = 0; i < g.nn[k]; ++i) {
+      int lo, cnt;
+      if (k < g.dim) axis_range(i, g.nn[k], 1, lo, cnt); else cnt = 1;
+      acc += cnt;
+      pref.push_back(acc);
+    }
+    g.T[k] = acc;
+  }
+  MRG_CUDA(cudaMallocAsync(&d_pref, pref.size() * sizeof(int64_t), s));
+  MRG_CUDA(cudaMemcpyAsync(d_pref, pref.data(), pref.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  for (int k = 0; k < 3; ++k) g.P[k] = d_pref + offs[k];
+  return MRG_OK;
+}
+
+template <typename T>
+void free_hier(Hier<T>* H, cudaStream_t s) {
+  if (!H) return;
+  if (H->graph) cudaGraphExecDestroy(H->graph);
+  if (H->bgraph) cudaGraphExecDestroy(H->bgraph);
+  for (void* ptr : {(void*)H->rh, (void*)H->v, (void*)H->sv, (void*)H->t, (void*)H->ph, (void*)H->sh})
+    if (ptr) cudaFreeAsync(ptr, s);
+  for (size_t l = 0; l < H->L.size(); ++l) {
+    HLevel& L = H->L[l];
+    if (l > 0) {
+      if (L.A) cudaFreeAsync(L.A, s);
+      if (L.d_pref) cudaFreeAsync(L.d_pref, s);
+      for (int k = 0; k < 2; ++k)
+        if (L.d_mid_pref[k]) cudaFreeAsync(L.d_mid_pref[k], s);
+    }
+    for (void* ptr : {L.minv, L.xa, L.xb, L.d, L.b, L.r})
+      if (ptr) cudaFreeAsync(ptr, s);
+  }
+  for (void* ptr : {(void*)H->mid[0], (void*)H->mid[1]})
+    if (ptr) cudaFreeAsync(ptr, s);
+  for (void* ptr : {(void*)H->cinv, (void*)H->lmax, (void*)H->err, (void*)H->x, (void*)H->r, (void*)H->p,
+                    (void*)H->q, (void*)H->parts, (void*)H->S})
+    if (ptr) cudaFreeAsync(ptr, s);
+  if (H->h_S) cudaFreeHost(H->h_S);
+  delete H;
+}
+
+// Builds the level structure (sizes, grids, buffers).  Values are computed by setup_values.
+template <typename T>
+int build_hier(const mrg_problem* p, Hier<T>*& out, cudaStream_t s) {
+  Hier<T>* H = new Hier<T>();
+  auto fail = [&](int rc) {
+    free_hier(H, s);
+    return rc;
+  };
+  HLevel L0;
+  L0.g = p->g;
+  L0.n = p->ndof;
+  L0.nnz = p->nnz;
+  H->L.push_back(L0);
+  // cell size per axis (box estimate); an axis is coarsened only while its cells are at most twice as
+  // long as the shortest ones (semi-coarsening keeps point smoothing effective on stretched grids)
+  double h[3] = {p->h[0], p->h[1], p->h[2]};
+  while ((int)H->L.size() < MAXLEV) {
+    const Grid& gf = H->L.back().g;
+    int nn[3], co[3] = {0, 0, 0}, any = 0;
+    double hmin = 1e300;
+    for (int k = 0; k < gf.dim; ++k) hmin = std::fmin(hmin, h[k]);
+    for (int pass = 0; pass < 2 && !any; ++pass)
+      for (int k = 0; k < gf.dim; ++k)
+        if (gf.nn[k] - 1 >= 3 && (pass == 1 || h[k] <= 2.0 * hmin * (1.0 + 1e-9))) {
+          co[k] = 1;
+          any = 1;
+        }
+    for (int k = 0; k < 3; ++k) {
+      nn[k] = gf.nn[k];
+      if (co[k]) {
+        nn[k] = (gf.nn[k] - 1 + 1) / 2 + 1;
+        h[k] *= 2.0;
+      }
+    }
+    const int64_t nfine = H->L.back().n;
+    if (!any || nfine <= MAXC) break;
+    HLevel Lc;
+    int rc = make_level_grid(gf, nn, s, Lc.g, Lc.d_pref);
+    if (rc) { H->L.push_back(Lc); return fail(rc); }
+    for (int k = 0; k < 3; ++k) Lc.X.co[k] = co[k];
+    // sweep plan: coarsen the axes one at a time; intermediate grids for all but the last sweep
+    int cur[3] = {gf.nn[0], gf.nn[1], gf.nn[2]};
+    for (int k = 0; k < 3; ++k)
+      if (co[k]) Lc.sweep_axis[Lc.nsweep++] = k;
+    for (int w = 0; w + 1 < Lc.nsweep; ++w) {
+      cur[Lc.sweep_axis[w]] = nn[Lc.sweep_axis[w]];
+      rc = make_level_grid(gf, cur, s, Lc.mid[w], Lc.d_mid_pref[w]);
+      if (rc) { H->L.push_back(Lc); return fail(rc); }
+    }
+    Lc.n = (int64_t)nn[0] * nn[1] * nn[2];
+    Lc.nnz = Lc.g.T[0] * Lc.g.T[1] * Lc.g.T[2];
+    H->L.push_back(Lc);
+  }
+  if (H->L.back().n > MAXC) return fail(mrg_fail(MRG_ENOTSUP, "multigrid: coarsest level too large"));
+  for (size_t l = 0; l < H->L.size(); ++l) {
+    HLevel& L = H->L[l];
+    const size_t vb = (size_t)L.n * sizeof(T);
+    if (l > 0 && cudaMallocAsync(&L.A, (size_t)L.nnz * sizeof(T), s) != cudaSuccess) return fail(mrg_fail(MRG_ENOMEM, "multigrid level matrix"));
+    for (void** ptr : {&L.minv, &L.xa, &L.xb, &L.d, &L.b, &L.r})
+      if (cudaMallocAsync(ptr, vb, s) != cudaSuccess) return fail(mrg_fail(MRG_ENOMEM, "multigrid level vectors"));
+  }
+  // scratch for the intermediate operators (largest over all levels)
+  size_t midmax[2] = {0, 0};
+  for (size_t l = 1; l < H->L.size(); ++l)
+    for (int w = 0; w + 1 < H->L[l].nsweep; ++w) {
+      const Grid& gm = H->L[l].mid[w];
+      midmax[w] = std::max(midmax[w], (size_t)(gm.T[0] * gm.T[1] * gm.T[2]));
+    }
+  for (int w = 0; w < 2; ++w)
+    if (midmax[w] && cudaMallocAsync(&H->mid[w], midmax[w] * sizeof(T), s) != cudaSuccess)
+      return fail(mrg_fail(MRG_ENOMEM, "multigrid Galerkin scratch"));
+  const int64_t n0 = p->ndof, nc = H->L.back().n;
+  const size_t nparts = (size_t)2 * grid_for(n0, 16) + 64;
+  if (cudaMallocAsync(&H->cinv, (size_t)nc * nc * sizeof(T), s) != cudaSuccess ||
+      cudaMallocAsync(&H->lmax, MAXLEV * sizeof(unsigned int), s) != cudaSuccess ||
+      cudaMallocAsync(&H->err, sizeof(int), s) != cudaSuccess ||
+      cudaMallocAsync(&H->x, n0 * sizeof(T), s) != cudaSuccess || cudaMallocAsync(&H->r, n0 * sizeof(T), s) != cudaSuccess ||
+      cudaMallocAsync(&H->p, n0 * sizeof(T), s) != cudaSuccess || cudaMallocAsync(&H->q, n0 * sizeof(T), s) != cudaSuccess ||
+      cudaMallocAsync(&H->parts, nparts * sizeof(double), s) != cudaSuccess ||
+      cudaMallocAsync(&H->S, sizeof(GScal), s) != cudaSuccess)
+    return fail(mrg_fail(MRG_ENOMEM, "multigrid workspace"));
+  if (cudaMallocHost(&H->h_S, sizeof(GScal)) != cudaSuccess) return fail(mrg_fail(MRG_ENOMEM, "multigrid pinned scalars"));
+  MRG_CUDA(cudaMemsetAsync(H->S, 0, sizeof(GScal), s));
+  MRG_CUDA(cudaMemsetAsync(H->parts, 0, nparts * sizeof(double), s));
+  out = H;
+  return MRG_OK;
+}
+
+template <typename T>
+LevDev<T> levdev(const HLevel& L) {
+  return LevDev<T>{L.g, L.n, (const T*)L.A, (T*)L.minv, (T*)L.xa, (T*)L.xb, (T*)L.d, (T*)L.b, (T*)L.r};
+}
+
+template <typename T>
+int set_staged_attr() {
+  static std::once_flag once;
+  static cudaError_t e = cudaSuccess;
+  std::call_once(once, [] {
+    const int smem = (NT / 32) * 2 * wbuf_elems<T>() * (int)sizeof(T);
+    e = cudaFuncSetAttribute(k_cheb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cg_spmv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bg_spmv<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bg_spmv<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  });
+  return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "multigrid smem attribute");
+}
+
+template <typename T>
+constexpr int staged_smem() { return (NT / 32) * 2 * wbuf_elems<T>() * (int)sizeof(T); }
+
+// Level operators, diagonals, Gershgorin bounds and the coarsest inverse for the Jacobian J.
+template <typename T>
+int setup_values(Hier<T>* H, const T* J, cudaStream_t s) {
+  H->L[0].A = const_cast<T*>(J);
+  MRG_CUDA(cudaMemsetAsync(H->lmax, 0, MAXLEV * sizeof(unsigned int), s));
+  MRG_CUDA(cudaMemsetAsync(H->err, 0, sizeof(int), s));
+  const int nl = (int)H->L.size();
+  for (int l = 0; l < nl; ++l) {
+    HLevel& L = H->L[l];
+    if (l > 0) {
+      const HLevel& F = H->L[l - 1];
+      const Grid* gin = &F.g;
+      const T* ain = (const T*)F.A;
+      for (int w = 0; w < L.nsweep; ++w) {
+        const bool last = (w + 1 == L.nsweep);
+        const Grid& gout = last ? L.g : L.mid[w];
+        T* aout = last ? (T*)L.A : H->mid[w];
+        const int64_t nout = (int64_t)gout.nn[0] * gout.nn[1] * gout.nn[2];
+        k_rap_axis<T><<<nblk(nout, NT), NT, 0, s>>>(*gin, gout, L.sweep_axis[w], ain, aout, H->err);
+        MRG_CUDA(cudaGetLastError());
+        gin = &gout;
+        ain = aout;
+      }
+    }
+    k_diag<T><<<nblk(L.n, NT), NT, 0, s>>>(L.g, (const T*)L.A, (T*)L.minv, H->lmax + l);
+    MRG_CUDA(cudaGetLastError());
+  }
+  k_coarse_inv<T><<<1, NT, 0, s>>>(H->L.back().g, (const T*)H->L.back().A, H->cinv, H->err);
+  MRG_CUDA(cudaGetLastError());
+  return MRG_OK;
+}
+
+// One V(NU, NU) cycle: out = M^{-1} in on level 0 (in, out: level-0 vectors not used by the cycle).
+template <typename T>
+void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
+  const int nl = (int)H->L.size();
+  const GScal* S = H->S;
+  for (int l = 0; l < nl - 1; ++l) {
+    LevDev<T> D = levdev<T>(H->L[l]);
+    if (l == 0) D.b = const_cast<T*>(in);
+    const unsigned gs = grid_for(D.n, staged_per_sm<T>()), ge = grid_for(D.n, 16);
+    // pre-smoothing from x = 0: xa <- step 0, xb <- step 1
+    k_cheb<T><<<ge, NT, 0, s>>>(D, D.xa, D.xa, 0, 1, H->lmax + l, S, H->err);
+    k_cheb<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xa, D.xb, 1, 0, H->lmax + l, S, H->err);
+    k_resid<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xb, S, H->err);
+    const HLevel& C = H->L[l + 1];
+    k_restrict<T><<<grid_for(C.n, 16), NT, 0, s>>>(D.g, C.g, C.X, D.r, (T*)C.b, S);
+  }
+  const HLevel& Lc = H->L[nl - 1];
+  k_coarse_apply<T><<<1, NT, 0, s>>>((int)Lc.n, H->cinv, (const T*)Lc.b, (T*)Lc.xb, S);
+  for (int l = nl - 2; l >= 0; --l) {
+    LevDev<T> D = levdev<T>(H->L[l]);
+    if (l == 0) D.b = const_cast<T*>(in);
+    const HLevel& C = H->L[l + 1];
+    const unsigned gs = grid_for(D.n, staged_per_sm<T>());
+    k_prolong<T><<<grid_for(D.n, 16), NT, 0, s>>>(D.g, C.g, C.X, (const T*)C.xb, D.xb, S);
+    // post-smoothing: xb -> xa (step 0), xa -> xb (step 1; level 0: -> out)
+    k_cheb<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xb, D.xa, 0, 0, H->lmax + l, S, H->err);
+    k_cheb<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xa, l == 0 ? out : D.xb, 1, 0, H->lmax + l, S, H->err);
+  }
+}
+
+template <typename T>
+CgVec<T> cgvec(Hier<T>* H) {
+  return CgVec<T>{H->x, H->r, H->p, H->q, (const T*)H->L[0].xb, H->parts, H->S};
+}
+
+template <typename T>
+void enqueue_iters(Hier<T>* H, int count, cudaStream_t s) {
+  const HLevel& L0 = H->L[0];
+  CgVec<T> V = cgvec(H);
+  const unsigned ge = grid_for(L0.n, 16), gs = grid_for(L0.n, staged_per_sm<T>());
+  for (int it = 0; it < count; ++it) {
+    k_cg_spmv<T><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    k_cg_update<T><<<ge, NT, 0, s>>>(L0.n, V);
+    enqueue_vcycle(H, H->r, (T*)H->L[0].xb, s);
+    k_cg_rz<T><<<ge, NT, 0, s>>>(L0.n, V, 0);
+  }
+}
+
+template <typename T>
+int finish_solve(mrg_problem* p, Hier<T>* H, cudaGraphExec_t graph, double* x, double rtol, int maxiter,
+                 mrg_solve_stats* st, cudaStream_t s, const char* what) {
+  const int64_t n = p->ndof;
+  const int max_chunks = maxiter / GCHUNK + 2;
+  for (int c = 0; c < max_chunks; ++c) {
+    MRG_CUDA(cudaGraphLaunch(graph, s));
+    MRG_CUDA(cudaMemcpyAsync(H->h_S, H->S, sizeof(GScal), cudaMemcpyDeviceToHost, s));
+    MRG_CUDA(cudaStreamSynchronize(s));
+    if (H->h_S->done) break;
+  }
+  int herr = 0;
+  MRG_CUDA(cudaMemcpyAsync(&herr, H->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  k_to_f64<T><<<nblk(n, 256), 256, 0, s>>>(n, H->x, x);
+  MRG_CUDA(cudaGetLastError());
+  MRG_CUDA(cudaStreamSynchronize(s));
+  const GScal* h = H->h_S;
+  if (st) {
+    st->iterations = h->iter;
+    st->outer_iterations = 0;
+    st->rel_residual = (h->r0 > 0) ? h->rnorm / h->r0 : 0.0;
+    st->abs_residual = h->rnorm;
+    st->status = h->status;
+  }
+  if (herr == 3 || h->status == MRG_ETIMEOUT) return mrg_fail(MRG_ETIMEOUT, std::string(what) + ": a staging copy timed out");
+  if (herr) return mrg_fail(MRG_ENUMERIC, "multigrid setup: singular coarse operator or transfer out of range");
+  if (h->status != MRG_OK) return mrg_fail(h->status, std::string(what) + ": breakdown or non-finite values");
+  if (h->r0 > 0 && h->rnorm / h->r0 > rtol) {
+    if (st) st->status = MRG_ENOCONV;
+    return mrg_fail(MRG_ENOCONV, std::string(what) + ": not converged within maxiter");
+  }
+  return MRG_OK;
+}
+
+template <typename T>
+int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
+           mrg_solve_stats* st, cudaStream_t s) {
+  int rc = set_staged_attr<T>();
+  if (rc) return rc;
+  rc = setup_values(H, J, s);
+  if (rc) return rc;
+  GScal init{};
+  init.tol = rtol;
+  init.maxiter = maxiter;
+  MRG_CUDA(cudaMemcpyAsync(H->S, &init, sizeof(GScal), cudaMemcpyHostToDevice, s));
+  const int64_t n = p->ndof;
+  CgVec<T> V = cgvec(H);
+  k_cg_init<T><<<grid_for(n, 16), NT, 0, s>>>(n, b, V);
+  MRG_CUDA(cudaGetLastError());
+  enqueue_vcycle(H, H->r, (T*)H->L[0].xb, s);
+  k_cg_rz<T><<<grid_for(n, 16), NT, 0, s>>>(n, V, 1);
+  MRG_CUDA(cudaGetLastError());
+  // captured chunk of iterations (re-captured when the Jacobian pointer or the stream changes)
+  if (!H->graph || H->graph_A != (const void*)J || H->graph_stream != s) {
+    if (H->graph) {
+      cudaGraphExecDestroy(H->graph);
+      H->graph = nullptr;
+    }
+    cudaStream_t cs = nullptr;
+    MRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      enqueue_iters(H, GCHUNK, cs);
+      e = cudaStreamEndCapture(cs, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&H->graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return mrg_cuda_check(e, "multigrid CG graph capture");
+    H->graph_A = J;
+    H->graph_stream = s;
+  }
+  return finish_solve(p, H, H->graph, x, rtol, maxiter, st, s, "multigrid CG");
+}
+
+template <typename T>
+BgVec<T> bgvec(Hier<T>* H) {
+  return BgVec<T>{H->x, H->r, H->rh, H->p, H->v, H->sv, H->t, H->ph, H->sh, H->parts, H->S};
+}
+
+template <typename T>
+void enqueue_bg_iters(Hier<T>* H, int count, cudaStream_t s) {
+  const HLevel& L0 = H->L[0];
+  BgVec<T> V = bgvec(H);
+  const unsigned ge = grid_for(L0.n, 16), gs = grid_for(L0.n, staged_per_sm<T>());
+  for (int it = 0; it < count; ++it) {
+    k_bg_p<T><<<ge, NT, 0, s>>>(L0.n, V);
+    enqueue_vcycle(H, H->p, H->ph, s);
+    k_bg_spmv<T, 0><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    k_bg_s<T><<<ge, NT, 0, s>>>(L0.n, V);
+    enqueue_vcycle(H, H->sv, H->sh, s);
+    k_bg_spmv<T, 1><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    k_bg_update<T><<<ge, NT, 0, s>>>(L0.n, V);
+  }
+}
+
+template <typename T>
+int gmg_bicgstab(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
+                 mrg_solve_stats* st, cudaStream_t s) {
+  int rc = set_staged_attr<T>();
+  if (rc) return rc;
+  const int64_t n = p->ndof;
+  if (!H->rh)
+    for (T** ptr : {&H->rh, &H->v, &H->sv, &H->t, &H->ph, &H->sh})
+      if (cudaMallocAsync(ptr, n * sizeof(T), s) != cudaSuccess) return mrg_fail(MRG_ENOMEM, "multigrid BiCGStab vectors");
+  rc = setup_values(H, J, s);
+  if (rc) return rc;
+  GScal init{};
+  init.tol = rtol;
+  init.maxiter = maxiter;
+  MRG_CUDA(cudaMemcpyAsync(H->S, &init, sizeof(GScal), cudaMemcpyHostToDevice, s));
+  k_bg_init<T><<<grid_for(n, 16), NT, 0, s>>>(n, b, bgvec(H));
+  MRG_CUDA(cudaGetLastError());
+  if (!H->bgraph || H->bgraph_A != (const void*)J || H->bgraph_stream != s) {
+    if (H->bgraph) {
+      cudaGraphExecDestroy(H->bgraph);
+      H->bgraph = nullptr;
+    }
+    cudaStream_t cs = nullptr;
+    MRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      enqueue_bg_iters(H, GCHUNK, cs);
+      e = cudaStreamEndCapture(cs, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&H->bgraph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return mrg_cuda_check(e, "multigrid BiCGStab graph capture");
+    H->bgraph_A = J;
+    H->bgraph_stream = s;
+  }
+  return finish_solve(p, H, H->bgraph, x, rtol, maxiter, st, s, "multigrid BiCGStab");
+}
+
+}  // namespace
+
+int mrg_gmg_kind(const mrg_problem* p) {
+  return p->gmg ? reinterpret_cast<const GmgData*>(p->gmg)->kind : MRG_PREC_JACOBI;
+}
+
+void mrg_gmg_free(mrg_problem* p) {
+  GmgData* G = reinterpret_cast<GmgData*>(p->gmg);
+  if (!G) return;
+  free_hier(G->h64, p->stream);
+  free_hier(G->h32, p->stream);
+  delete G;
+  p->gmg = nullptr;
+}
+
+// Solves J x = b (x0 = 0) with multigrid-preconditioned CG in the precision of J; x receives the FP64
+// solution.
+int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
+                  mrg_solve_stats* st, cudaStream_t s) {
+  if (p->g.p != 1) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 problems only");
+  GmgData* G = gdata(p);
+  int rc;
+  if (fp32) {
+    if (!G->h32 && (rc = build_hier<float>(p, G->h32, s))) return rc;
+    return gmg_cg<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, s);
+  }
+  if (!G->h64 && (rc = build_hier<double>(p, G->h64, s))) return rc;
+  return gmg_cg<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, s);
+}
+
+// Same for a nonsymmetric J: right-preconditioned BiCGStab with the multigrid V-cycle.
+int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
+                     mrg_solve_stats* st, cudaStream_t s) {
+  if (p->g.p != 1) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 problems only");
+  GmgData* G = gdata(p);
+  int rc;
+  if (fp32) {
+    if (!G->h32 && (rc = build_hier<float>(p, G->h32, s))) return rc;
+    return gmg_bicgstab<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, s);
+  }
+  if (!G->h64 && (rc = build_hier<double>(p, G->h64, s))) return rc;
+  return gmg_bicgstab<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, s);
+}
+
+extern "C" int mrg_set_preconditioner(mrg_problem* p, int32_t kind) {
+  if (!p) return mrg_fail(MRG_EINVAL, "mrg_set_preconditioner: null problem");
+  if (kind != MRG_PREC_JACOBI && kind != MRG_PREC_GMG)
+    return mrg_fail(MRG_EINVAL, "mrg_set_preconditioner: unknown preconditioner");
+  if (kind == MRG_PREC_GMG && p->g.p != 1) return mrg_fail(MRG_ENOTSUP, "multigrid preconditioner: Q1 problems only");
+  gdata(p)->kind = kind;
+  return MRG_OK;
+}

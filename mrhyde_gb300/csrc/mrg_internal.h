@@ -102,6 +102,7 @@ struct mrg_problem {
   void* q2 = nullptr;            // Q2 tensor-product data (mrg_assemble_q2.cu)
   void* bicg = nullptr;          // BiCGStab workspace (mrg_bicgstab.cu)
   void* bnd = nullptr;           // face boundary conditions (mrg_boundary.cu)
+  void* gmg = nullptr;           // multigrid hierarchy and preconditioner choice (mrg_gmg.cu)
   cudaStream_t stream = nullptr;       // creation stream: the handle's memory is allocated/freed in its order
   cudaStream_t last_stream = nullptr;  // last stream work was enqueued on (drained before destroy)
   SolverWork* work = nullptr;
@@ -139,6 +140,13 @@ bool mrg_boundary_active(const mrg_problem* p);
 int mrg_launch_boundary(mrg_problem* p, const double* u, double* r, void* J, bool fp32, cudaStream_t s);
 // 1-D Lagrange basis of degree p on equispaced nodes of [-1,1]: values l[0..p], derivatives dl[0..p]
 void mrg_lagrange_1d(int p, double xi, double* l, double* dl);
+// Multigrid preconditioned CG (mrg_gmg.cu)
+int mrg_gmg_kind(const mrg_problem* p);
+void mrg_gmg_free(mrg_problem* p);
+int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
+                  mrg_solve_stats* st, cudaStream_t s);
+int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
+                     mrg_solve_stats* st, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);
 int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s);  // res = b - res

@@ -178,6 +178,7 @@ static void free_problem(mrg_problem* p) {
   mrg_bicg_free(p);
   mrg_q2_free(p);
   mrg_boundary_free(p);
+  mrg_gmg_free(p);
   cudaFreeAsync(p->d_prefix, s);
   cudaFreeAsync(p->d_kappa, s);
   cudaFreeAsync(p->d_kappa32, s);

@@ -22,14 +22,18 @@
 // iteration), dot products are accumulated in FP64 per block; the Newton residual, the update of u
 // and the stopping test stay FP64, so Newton / iterative refinement recovers the FP64 solution.
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
+#include "mrg_device.cuh"
 #include "mrg_internal.h"
 
 namespace {
 
-constexpr int ST = 128;          // rows per CTA
+using namespace mrgdev;
+
+constexpr int ST = WST;          // rows per CTA
 constexpr int CHUNK = 16;        // PCG iterations per captured graph
 
 // device scalars of one PCG instance
@@ -40,419 +44,26 @@ struct PcgScal {
   int pad;
 };
 
-__device__ __forceinline__ void decompose(const Grid& g, int64_t n, int& ix, int& iy, int& iz) {
-  // 32-bit arithmetic: n_dofs <= INT32_MAX is enforced by mrg_problem_create
-  const unsigned un = (unsigned)n, nx = (unsigned)g.nn[0], ny = (unsigned)g.nn[1];
-  const unsigned t = un / nx;
-  ix = (int)(un - t * nx);
-  iy = (int)(t % ny);
-  iz = (int)(t / ny);
-}
-
-// Load the CSR segment [seg0, seg1) of a CTA's contiguous rows into shared memory with 16-byte
-// streaming loads.  dst has the same address phase modulo 16 bytes as src.
-template <typename T>
-__device__ __forceinline__ void seg_load(const T* __restrict__ src, T* __restrict__ dst, int64_t len) {
-  constexpr int V = 16 / sizeof(T);
-  int head = (int)(((16 - ((uintptr_t)src & 15)) & 15) / sizeof(T));
-  if (head > len) head = (int)len;
-  for (int k = threadIdx.x; k < head; k += blockDim.x) dst[k] = __ldcs(src + k);
-  const int64_t body = (len - head) / V;
-  if constexpr (sizeof(T) == 8) {
-    const double2* s2 = reinterpret_cast<const double2*>(src + head);
-    double2* d2 = reinterpret_cast<double2*>(dst + head);
-    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) d2[v] = __ldcs(s2 + v);
-  } else {
-    const float4* s4 = reinterpret_cast<const float4*>(src + head);
-    float4* d4 = reinterpret_cast<float4*>(dst + head);
-    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) d4[v] = __ldcs(s4 + v);
-  }
-  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) dst[k] = __ldcs(src + k);
-}
-
-
-
-struct RowInfo {
-  int lx, ly, lz, cx, cy, cz;
-  int64_t rp;
-};
-
-// PC > 0: the polynomial order is a compile-time constant (the axis divisions fold away)
-template <int PC = 0>
-__device__ __forceinline__ RowInfo row_info(const Grid& g, int ix, int iy, int iz) {
-  RowInfo R;
-  const int p = PC > 0 ? PC : g.p;
-  axis_range(ix, g.nn[0], p, R.lx, R.cx);
-  axis_range(iy, g.nn[1], p, R.ly, R.cy);
-  if (g.dim == 3) axis_range(iz, g.nn[2], p, R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
-  R.rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)R.cz * (g.P[1][iy] * g.T[0] + (int64_t)R.cy * g.P[0][ix]);
-  return R;
-}
-
-__device__ __forceinline__ int64_t row_ptr_at(const Grid& g, int64_t n, int64_t nrows) {
-  if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
-  int ix, iy, iz;
-  decompose(g, n, ix, iy, iz);
-  return row_info(g, ix, iy, iz).rp;
-}
-
-// Stages the values of the CTA's rows in shared memory (P = 1: at most 27 per row, contiguous in
-// CSR) and returns the staged copy of the row starting at my_rp; for P = 2 returns the row in global
-// memory.  Every thread of the CTA must call it (it synchronises the block).
-template <int P, typename JT>
-__device__ __forceinline__ const JT* stage_rows(const Grid& g, int64_t nrows, const JT* __restrict__ J,
-                                                int64_t my_rp, unsigned char* smem_raw, int64_t tile) {
-  if constexpr (P != 1) {
-    return J + my_rp;
-  } else {
-    const int64_t n0 = tile * ST;
-    const int64_t n1 = (n0 + ST < nrows) ? n0 + ST : nrows;
-    const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
-    const int phase = (int)(((uintptr_t)(J + seg0) & 15) / sizeof(JT));
-    JT* sv = reinterpret_cast<JT*>(smem_raw) + phase;
-    seg_load<JT>(J + seg0, sv, seg1 - seg0);
-    __syncthreads();
-    return sv + (my_rp - seg0);
-  }
-}
-
-template <int P, typename JT>
-constexpr int stage_bytes() {
-  return P == 1 ? (ST * 27 + 16 / (int)sizeof(JT)) * (int)sizeof(JT) : 0;
-}
-
-// Double-buffered staging for the PCG SpMV (P = 1): tile t's CSR segment is copied into shared
-// memory with cp.async (16-byte, L2-only) while tile t - G is being multiplied.  The ragged head and
-// tail of a segment (not 16-byte aligned) are copied with plain loads.
-constexpr int STAGE_ELEMS_PAD = 4;
-template <typename JT>
-constexpr int stage_elems() { return ST * 27 + STAGE_ELEMS_PAD; }
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// issues the copy of `tile`'s segment into buf; returns seg0
-template <typename JT>
-__device__ __forceinline__ int64_t tile_issue(const Grid& g, int64_t nrows, const JT* __restrict__ J, int64_t tile,
-                                              JT* buf) {
-  const int64_t n0 = tile * ST;
-  const int64_t n1 = (n0 + ST < nrows) ? n0 + ST : nrows;
-  const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
-  const JT* src = J + seg0;
-  JT* dst = buf + (int)(((uintptr_t)src & 15) / sizeof(JT));
-  const int64_t len = seg1 - seg0;
-  constexpr int V = 16 / sizeof(JT);
-  int head = (int)(((16 - ((uintptr_t)src & 15)) & 15) / sizeof(JT));
-  if (head > len) head = (int)len;
-  const int64_t body = (len - head) / V;
-  for (int k = threadIdx.x; k < head; k += blockDim.x) dst[k] = __ldcs(src + k);
-  for (int64_t v = threadIdx.x; v < body; v += blockDim.x) cp_async16(dst + head + v * V, src + head + v * V);
-  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) dst[k] = __ldcs(src + k);
-  cp_async_commit();
-  return seg0;
-}
-
-// ---- per-warp staged rows (P = 1) --------------------------------------------------------------
-// A warp owns tiles of 32 consecutive rows.  Their CSR values form one contiguous segment, which lane 0
-// copies into the warp's own shared buffer with a 1-D bulk copy (cp.async.bulk, completion counted on
-// the warp's mbarrier) while the warp multiplies its previous tile; the unaligned ends of the segment
-// are copied with plain loads.  No CTA-wide barrier is involved, so warps never wait for each other.
-constexpr int WROWS = 32;
-template <typename JT>
-__host__ __device__ constexpr int wbuf_elems() { return WROWS * 27 + 2 * (16 / (int)sizeof(JT)); }
-template <typename JT>
-constexpr int wspmv_smem() { return (ST / 32) * 2 * wbuf_elems<JT>() * (int)sizeof(JT); }
-
-constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on one tile's copy
-
-__device__ __forceinline__ bool wbar_try(uint32_t mbar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(mbar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t wtimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
-  return t;
-}
-
-// bounded wait by every lane of the warp; the result is warp-uniform
-__device__ __forceinline__ bool wbar_wait(uint32_t mbar, uint32_t parity) {
-  int ok = 1;
-  if (!wbar_try(mbar, parity)) {
-    const uint64_t t0 = wtimer();
-    while (!wbar_try(mbar, parity))
-      if (wtimer() - t0 > WAIT_NS) { ok = 0; break; }
-  }
-  return __all_sync(0xffffffffu, ok) != 0;
-}
-
-// Issues the copy of warp tile `tile` into buf; returns the global byte address mapped to buf[0].
-template <typename JT>
-__device__ __forceinline__ uintptr_t wtile_issue(const Grid& g, int64_t nrows, const JT* __restrict__ J, int64_t tile,
-                                                 JT* buf, uint32_t mbar, int lane) {
-  const int64_t n0 = tile * WROWS;
-  const int64_t n1 = (n0 + WROWS < nrows) ? n0 + WROWS : nrows;
-  const int64_t nnz = g.T[0] * g.T[1] * g.T[2];
-  const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
-  const uintptr_t lo = (uintptr_t)(J + seg0), hi = (uintptr_t)(J + seg1);
-  const uintptr_t base = lo & ~(uintptr_t)15;
-  const uintptr_t jb = ((uintptr_t)J + 15) & ~(uintptr_t)15, je = (uintptr_t)(J + nnz) & ~(uintptr_t)15;
-  uintptr_t b0 = base < jb ? jb : base;
-  uintptr_t b1 = (hi + 15) & ~(uintptr_t)15;
-  if (b1 > je) b1 = je;
-  if (b0 > hi) b0 = hi;
-  if (b1 < b0) b1 = b0;
-  unsigned char* sb = reinterpret_cast<unsigned char*>(buf);
-  // plain loads: head [lo, b0) and tail [max(b1, lo), hi) -- a few elements at most
-  constexpr int E = (int)sizeof(JT);
-  const int nhead = (int)((b0 - lo) / E);
-  const uintptr_t t0 = b1 > lo ? b1 : lo;
-  const int ntail = (int)((hi - t0) / E);
-  if (lane < nhead) *reinterpret_cast<JT*>(sb + (lo - base) + lane * E) = __ldcs(reinterpret_cast<const JT*>(lo) + lane);
-  if (lane >= 8 && lane - 8 < ntail)
-    *reinterpret_cast<JT*>(sb + (t0 - base) + (lane - 8) * E) = __ldcs(reinterpret_cast<const JT*>(t0) + (lane - 8));
-  if (lane == 0) {
-    const uint32_t bytes = (uint32_t)(b1 - b0);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
-    if (bytes)
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-              (uint32_t)__cvta_generic_to_shared(sb + (b0 - base))),
-          "l"(b0), "r"(bytes), "r"(mbar)
-          : "memory");
-  }
-  return base;
-}
-
-// Runs f(n, R, vals) for every row n (vals = the row's values in shared memory), warp-tiled and
-// double-buffered.  Returns false if a copy did not complete within the time bound.
-template <typename JT, typename F>
-__device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, const JT* __restrict__ J,
-                                                 unsigned char* smem_raw, uint64_t* mbar_base, F&& f) {
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  JT* const buf0 = reinterpret_cast<JT*>(smem_raw) + (2 * w) * wbuf_elems<JT>();
-  JT* const buf1 = buf0 + wbuf_elems<JT>();
-  const uint32_t mb0 = (uint32_t)__cvta_generic_to_shared(mbar_base + 2 * w), mb1 = mb0 + 8u;
-  if (lane == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb1) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  __syncwarp();
-  const int64_t ntiles = (nrows + WROWS - 1) / WROWS;
-  const int64_t W = (int64_t)gridDim.x * (ST / 32);
-  int64_t tile = (int64_t)blockIdx.x * (ST / 32) + w;
-  // buffer b of the current tile; the other buffer receives the next tile
-  uintptr_t base0 = 0, base1 = 0;
-  uint32_t ph0 = 0u, ph1 = 0u;
-  bool armed0 = false, armed1 = false, ok = true;
-  int b = 0;
-  if (tile < ntiles) {
-    base0 = wtile_issue<JT>(g, nrows, J, tile, buf0, mb0, lane);
-    armed0 = true;
-  }
-  for (; tile < ntiles; tile += W) {
-    const int64_t nxt = tile + W;
-    if (nxt < ntiles) {
-      if (b == 0) { base1 = wtile_issue<JT>(g, nrows, J, nxt, buf1, mb1, lane); armed1 = true; }
-      else        { base0 = wtile_issue<JT>(g, nrows, J, nxt, buf0, mb0, lane); armed0 = true; }
-    }
-    const bool got = (b == 0) ? wbar_wait(mb0, ph0) : wbar_wait(mb1, ph1);
-    if (!got) { ok = false; break; }
-    if (b == 0) { ph0 ^= 1u; armed0 = false; } else { ph1 ^= 1u; armed1 = false; }
-    __syncwarp();
-    const int64_t n = tile * WROWS + lane;
-    if (n < nrows) {
-      int ix, iy, iz;
-      decompose(g, n, ix, iy, iz);
-      const RowInfo R = row_info<1>(g, ix, iy, iz);
-      const unsigned char* cb = reinterpret_cast<const unsigned char*>(b == 0 ? buf0 : buf1);
-      const JT* vals = reinterpret_cast<const JT*>(cb + ((uintptr_t)(J + R.rp) - (b == 0 ? base0 : base1)));
-      f(n, R, vals);
-    }
-    __syncwarp();
-    b ^= 1;
-  }
-  if (!ok) {  // let copies still in flight land before the CTA exits (bounded)
-    if (armed0) wbar_wait(mb0, ph0);
-    if (armed1) wbar_wait(mb1, ph1);
-  }
-  return ok;
-}
-
-// sum of v over the block, returned in thread 0 (FP64)
-__device__ __forceinline__ double block_sum(double v) {
-  __shared__ double sh[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) sh[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
-  __syncthreads();
-  return s;
-}
-
-__device__ __forceinline__ double block_max(double v) {
-  __shared__ double sh[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) sh[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = fmax(s, sh[i]);
-  __syncthreads();
-  return s;
-}
-
-// Last-block reduction: each block stores its partials; the block that increments the counter last
-// sums all partials in index order (deterministic) and runs `fin`.  Returns true in that block.
-template <int K>
-__device__ __forceinline__ bool last_block(double* parts, const double (&mine)[K], unsigned int* counter) {
-  __shared__ bool amlast;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) parts[(size_t)k * gridDim.x + blockIdx.x] = mine[k];
-    __threadfence();
-    unsigned int prev = atomicAdd(counter, 1u);
-    amlast = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  return amlast;
-}
-
-template <int K>
-__device__ __forceinline__ void sum_parts(const double* parts, double (&out)[K], unsigned int* counter) {
-  // whole block cooperates; fixed order: thread t sums indices t, t+blockDim, ... with 4 independent
-  // accumulators (combined in a fixed order), then the block tree.  The partials were published by
-  // the other blocks before their fence + counter increment; ld.global.cg reads them from L2, and the
-  // loads are independent so they pipeline instead of forming a chain of L2 round trips.
-  for (int k = 0; k < K; ++k) {
-    const double* pk = parts + (size_t)k * gridDim.x;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    unsigned int i = threadIdx.x;
-    const unsigned int st = blockDim.x;
-    for (; i + 3 * st < gridDim.x; i += 4 * st) {
-      s0 += __ldcg(pk + i);
-      s1 += __ldcg(pk + i + st);
-      s2 += __ldcg(pk + i + 2 * st);
-      s3 += __ldcg(pk + i + 3 * st);
-    }
-    for (; i < gridDim.x; i += st) s0 += __ldcg(pk + i);
-    double s = block_sum((s0 + s1) + (s2 + s3));
-    out[k] = s;  // valid in thread 0
-  }
-  if (threadIdx.x == 0) *counter = 0u;
-}
-
-// ------------------------------------------------------------------------------------------------
-// row kernels: y_i = sum_j J_ij x_j over the row of node i
-// ------------------------------------------------------------------------------------------------
-template <int P, typename JT, typename XT>
-__device__ __forceinline__ double row_apply(const Grid& g, const RowInfo& R, const JT* __restrict__ vals,
-                                            const XT* __restrict__ x) {
-  constexpr int MC = 2 * P + 1;
-  const int64_t NX = g.nn[0], plane = (int64_t)g.nn[0] * g.nn[1];
-  if (P == 1 && R.cx == 3 && R.cy == 3 && R.cz == 3) {
-    // interior row: all 27 couplings, no predicates, so all loads issue before the FMAs
-    const XT* xb = x + R.lx + NX * R.ly + plane * R.lz;
-    double xv[27];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) xv[k] = (double)__ldg(xb + (k % 3) + NX * ((k / 3) % 3) + plane * (k / 9));
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < 27; ++k) acc = fma((double)vals[k], xv[k], acc);
-    return acc;
-  }
-  double acc = 0.0;
-  int pos = 0;
-#pragma unroll
-  for (int z = 0; z < (P == 1 ? 3 : MC); ++z) {
-    if (z < R.cz) {
-#pragma unroll
-      for (int y = 0; y < MC; ++y) {
-        if (y < R.cy) {
-          const int64_t base = (R.lx) + NX * (R.ly + y) + plane * (R.lz + z);
-#pragma unroll
-          for (int xo = 0; xo < MC; ++xo)
-            if (xo < R.cx) {
-              acc = fma((double)vals[pos], (double)__ldg(x + base + xo), acc);
-              ++pos;
-            }
-        }
-      }
-    }
-  }
-  return acc;
-}
-
-// FP32 variant accumulating in FP32 (inner solve of the mixed path)
-template <int P>
-__device__ __forceinline__ float row_apply_f(const Grid& g, const RowInfo& R, const float* __restrict__ vals,
-                                             const float* __restrict__ x) {
-  constexpr int MC = 2 * P + 1;
-  const int64_t NX = g.nn[0], plane = (int64_t)g.nn[0] * g.nn[1];
-  if (P == 1 && R.cx == 3 && R.cy == 3 && R.cz == 3) {
-    const float* xb = x + R.lx + NX * R.ly + plane * R.lz;
-    float xv[27];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) xv[k] = __ldg(xb + (k % 3) + NX * ((k / 3) % 3) + plane * (k / 9));
-    float acc = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 27; ++k) acc = fmaf(vals[k], xv[k], acc);
-    return acc;
-  }
-  float acc = 0.0f;
-  int pos = 0;
-#pragma unroll
-  for (int z = 0; z < MC; ++z) {
-    if (z < R.cz) {
-#pragma unroll
-      for (int y = 0; y < MC; ++y) {
-        if (y < R.cy) {
-          const int64_t base = (R.lx) + NX * (R.ly + y) + plane * (R.lz + z);
-#pragma unroll
-          for (int xo = 0; xo < MC; ++xo)
-            if (xo < R.cx) {
-              acc = fmaf(vals[pos], __ldg(x + base + xo), acc);
-              ++pos;
-            }
-        }
-      }
-    }
-  }
-  return acc;
-}
-
+// y = J x (FP64 accumulation); Q1 rows through the per-warp staged loop.  err (may be null) is set to
+// 1 if a staging copy did not complete within its time bound.
 template <int P, typename JT>
 __global__ void __launch_bounds__(ST) k_spmv(Grid g, int64_t nrows, const JT* __restrict__ J, const double* __restrict__ x,
-                                             double* __restrict__ y) {
+                                             double* __restrict__ y, int* err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x;
-  const bool act = n < nrows;
-  RowInfo R{};
-  if (act) {
-    int ix, iy, iz;
-    decompose(g, n, ix, iy, iz);
-    R = row_info<P>(g, ix, iy, iz);
+  __shared__ __align__(8) uint64_t mbar[2 * (ST / 32)];
+  if constexpr (P == 1) {
+    const bool ok = warp_staged_rows<JT>(g, nrows, J, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const JT* vals) {
+      y[n] = row_apply<1, JT, double>(g, R, vals, x);
+    });
+    if (!ok && err) atomicExch(err, 1);
+  } else {
+    for (int64_t n = (int64_t)blockIdx.x * ST + threadIdx.x; n < nrows; n += (int64_t)gridDim.x * ST) {
+      int ix, iy, iz;
+      decompose(g, n, ix, iy, iz);
+      const RowInfo R = row_info<P>(g, ix, iy, iz);
+      y[n] = row_apply<P, JT, double>(g, R, J + R.rp, x);
+    }
   }
-  const JT* vals = stage_rows<P, JT>(g, nrows, J, R.rp, smem_raw, blockIdx.x);
-  if (act) y[n] = row_apply<P, JT, double>(g, R, vals, x);
 }
 
 // ---- FP64 PCG kernels ---------------------------------------------------------------------------
@@ -1015,16 +626,29 @@ extern "C" int mrg_spmv(const mrg_problem* p, const void* J, int32_t fp32, const
                         mrg_stream_t stream) {
   if (!p || !J || !x || !y) return mrg_fail(MRG_EINVAL, "mrg_spmv: null argument");
   cudaStream_t s = (cudaStream_t)stream;
-  const unsigned nb = nblk(p->ndof, ST);
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once, [] {
+    attr_err = cudaFuncSetAttribute(k_spmv<1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, spmv_smem<1, double>());
+    if (attr_err == cudaSuccess)
+      attr_err = cudaFuncSetAttribute(k_spmv<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, spmv_smem<1, float>());
+  });
+  MRG_CUDA(attr_err);
   if (p->g.p == 1) {
-    if (fp32) k_spmv<1, float><<<nb, ST, stage_bytes<1, float>(), s>>>(p->g, p->ndof, (const float*)J, x, y);
-    else k_spmv<1, double><<<nb, ST, stage_bytes<1, double>(), s>>>(p->g, p->ndof, (const double*)J, x, y);
+    if (fp32) k_spmv<1, float><<<pcg_grid(p, spmv_per_sm<1, float>()), ST, spmv_smem<1, float>(), s>>>(p->g, p->ndof, (const float*)J, x, y, nullptr);
+    else k_spmv<1, double><<<pcg_grid(p, spmv_per_sm<1, double>()), ST, spmv_smem<1, double>(), s>>>(p->g, p->ndof, (const double*)J, x, y, nullptr);
   } else {
-    if (fp32) k_spmv<2, float><<<nb, ST, 0, s>>>(p->g, p->ndof, (const float*)J, x, y);
-    else k_spmv<2, double><<<nb, ST, 0, s>>>(p->g, p->ndof, (const double*)J, x, y);
+    if (fp32) k_spmv<2, float><<<pcg_grid(p), ST, 0, s>>>(p->g, p->ndof, (const float*)J, x, y, nullptr);
+    else k_spmv<2, double><<<pcg_grid(p), ST, 0, s>>>(p->g, p->ndof, (const double*)J, x, y, nullptr);
   }
   MRG_CUDA(cudaGetLastError());
   return MRG_OK;
+}
+
+// res = b - res
+__global__ void k_b_minus(int64_t n, const double* __restrict__ b, double* __restrict__ res) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) res[i] = b[i] - res[i];
 }
 
 extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const double* b, double* x, double rtol,
@@ -1033,6 +657,22 @@ extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const 
   if (!(rtol >= 0.0) || maxiter < 0) return mrg_fail(MRG_EINVAL, "mrg_solve_pcg: bad tolerance or iteration limit");
   cudaStream_t s = (cudaStream_t)stream;
   p->last_stream = s;
+  if (mrg_gmg_kind(p) == MRG_PREC_GMG) {
+    // multigrid CG on the correction: dx solves J dx = b - J x0, then x = x0 + dx
+    int rc = ensure_work(p, true, false, s);
+    if (rc) return rc;
+    SolverWork* w = p->work;
+    rc = mrg_spmv(p, J, fp32, x, w->r, stream);
+    if (rc) return rc;
+    k_b_minus<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, b, w->r);
+    MRG_CUDA(cudaGetLastError());
+    rc = mrg_gmg_solve(p, J, fp32 != 0, w->r, w->z, rtol, maxiter, st, s);
+    if (rc && rc != MRG_ENOCONV) return rc;
+    k_axpy<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, 1.0, w->z, x);
+    MRG_CUDA(cudaGetLastError());
+    MRG_CUDA(cudaStreamSynchronize(s));
+    return rc;
+  }
   if (!fp32) return pcg64(p, (const double*)J, b, x, rtol, maxiter, st, s);
   // FP32 matrix: solve J dx = b - J x0 in FP32, then x = x0 + dx
   int rc = ensure_work(p, true, true, s);
@@ -1054,10 +694,6 @@ extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const 
   return MRG_OK;
 }
 
-__global__ void k_b_minus(int64_t n, const double* __restrict__ b, double* __restrict__ res) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) res[i] = b[i] - res[i];
-}
 
 int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s) {
   k_b_minus<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, b, res);
@@ -1127,7 +763,11 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
       mrg_solve_stats ls{};
       // the 1+u^2 Jacobian is nonsymmetric (2 u phi_j grad u . grad phi_i): BiCGStab; CG otherwise
       const bool bicg = (o->krylov == MRG_KRYLOV_BICGSTAB) || (o->krylov == MRG_KRYLOV_AUTO && p->kind != MRG_THERMAL);
-      if (!mixed) {
+      if (mrg_gmg_kind(p) == MRG_PREC_GMG) {
+        rc = bicg ? mrg_gmg_bicgstab(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s)
+                  : mrg_gmg_solve(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s);
+        if (rc && rc != MRG_ENOCONV && !(bicg && rc == MRG_ENUMERIC)) return rc;
+      } else if (!mixed) {
         MRG_CUDA(cudaMemsetAsync(w->du, 0, p->ndof * sizeof(double), s));
         rc = bicg ? mrg_bicg_solve64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s)
                   : pcg64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s);
@@ -1191,7 +831,6 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
 //     that device current; make that first call before any stream capture on the device.
 // ------------------------------------------------------------------------------------------------
-#include <mutex>
 
 namespace {
 constexpr int64_t NA_N = MRG_NOALLOC_MAX_DOFS;

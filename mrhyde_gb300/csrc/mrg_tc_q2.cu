@@ -360,13 +360,36 @@ __device__ __forceinline__ void pair_cells(int i, int j, int nc, int& lo, int& h
   if (hi > nc - 1) hi = nc - 1;
 }
 
-constexpr int GT = 256;  // gather threads per CTA (8 rows in flight)
+constexpr int GT = 256;   // gather threads per CTA
+constexpr int GRUN = 16;  // consecutive rows a warp takes at a time
 
-// One warp per CSR row.  Lane l < 27 stands for local column node l of a cell: for each of the row's
-// cells (at most 8, in the fixed order cz, cy, cx) it loads E_c[l_i][l] -- a contiguous run of 27 values
-// -- and adds it to the row's entry of that column in a per-warp shared row.  All loads of a row are
-// issued before the first add; the adds are ordered by cell, so every entry is summed in the same fixed
-// order on every run.  The row is then written once, coalesced.
+// Row-gather of one CSR row from its NX x NY x NZ boundary-cell block (NX, NY, NZ in {1, 2}).  Lane l < 27
+// stands for local column node l of a cell: for each of the row's cells (fixed order cz, cy, cx) it loads
+// E_c[l_i][l] -- a contiguous run of 27 values -- and adds it to the row's entry of that column in the
+// warp's shared row.  All loads of the row are issued before the first add; the adds are ordered by cell,
+// so every entry is summed in the same fixed order on every run.  The row is then written once,
+// coalesced.
+template <int NX, int NY, int NZ>
+__device__ __forceinline__ void gather_cells(float* __restrict__ rb, const float* __restrict__ e0, int sy, int sz,
+                                             int li0, int pos0, int cy, int cx, bool col, int lane) {
+  constexpr int NC = NX * NY * NZ;
+  float v[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const int kx = k % NX, ky = (k / NX) % NY, kz = k / (NX * NY);
+    const int li = li0 - 2 * (kx + 3 * ky + 9 * kz);
+    v[k] = col ? __ldg(e0 + kx * NE + ky * sy + kz * sz + li * 28) : 0.0f;
+  }
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const int kx = k % NX, ky = (k / NX) % NY, kz = k / (NX * NY);
+    if (col) rb[pos0 + 2 * ((kz * cy + ky) * cx + kx)] += v[k];
+    __syncwarp();
+  }
+}
+
+// One warp per CSR row, GRUN consecutive rows at a time (coordinates and row pointers advance
+// incrementally along the run; a new run starts from a full decomposition).
 __global__ void __launch_bounds__(GT) k_q2_gather(Grid g, int64_t nrows, const float* __restrict__ E,
                                                   float* __restrict__ J, int ovw) {
   __shared__ float rows[GT / 32][128];
@@ -375,59 +398,57 @@ __global__ void __launch_bounds__(GT) k_q2_gather(Grid g, int64_t nrows, const f
   const int64_t wid = ((int64_t)blockIdx.x * GT + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * GT) >> 5;
   const int ncx = g.nc[0], ncy = g.nc[1];
+  const int sy = ncx * NE, sz = ncx * ncy * NE;  // cell strides (host checks they fit in 32 bits)
   const bool col = lane < 27;
   const int ljx = lane % 3, ljy = (lane / 3) % 3, ljz = lane / 9;
-  for (int64_t n = wid; n < nrows; n += nw) {
+  for (int64_t r0 = wid * GRUN; r0 < nrows; r0 += nw * GRUN) {
     int ix, iy, iz;
-    mrgdev::decompose(g, n, ix, iy, iz);
-    const mrgdev::RowInfo R = mrgdev::row_info<2>(g, ix, iy, iz);
-    const int len = R.cx * R.cy * R.cz;
-    float* row = J + R.rp;
-    if (node_fixed(g, ix, iy, iz)) {
-      const int dg = (int)(mrgdev::diag_pos(R, ix, iy, iz) - R.rp);
-      if (ovw) {
-        for (int e = lane; e < len; e += 32) __stcs(row + e, e == dg ? 1.0f : 0.0f);
-      } else if (lane == 0) {
-        row[dg] = 1.0f;
-      }
-      continue;
-    }
-    int fx, fy, fz, nxc, nyc, nzc;
-    axis_cells(ix, g.nn[0], 2, fx, nxc);
-    axis_cells(iy, g.nn[1], 2, fy, nyc);
-    axis_cells(iz, g.nn[2], 2, fz, nzc);
-    const int ncells = nxc * nyc * nzc;
-    // cell (fx+kx, fy+ky, fz+kz): local row index li0 - 2 (kx + 3 ky + 9 kz), row position of this
-    // lane's column pos0 + 2 (kz cy cx + ky cx + kx), cell index cell0 + kx + ncx (ky + ncy kz)
-    const int li0 = (ix - 2 * fx) + 3 * (iy - 2 * fy) + 9 * (iz - 2 * fz);
-    const int pos0 = ((2 * fz + ljz - R.lz) * R.cy + (2 * fy + ljy - R.ly)) * R.cx + (2 * fx + ljx - R.lx);
-    const float* e0 = E + (fx + (int64_t)ncx * (fy + (int64_t)ncy * fz)) * NE + lane;
-    const int64_t sy = (int64_t)ncx * NE, sz = (int64_t)ncx * ncy * NE;
-    float v[8];
-    int pos[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      // k -> (kx, ky, kz), x fastest
-      const int kx = (nxc == 2) ? (k & 1) : 0, k2 = (nxc == 2) ? (k >> 1) : k;
-      const int ky = (nyc == 2) ? (k2 & 1) : 0, kz = (nyc == 2) ? (k2 >> 1) : k2;
-      const int li = li0 - 2 * (kx + 3 * ky + 9 * kz);
-      const bool on = col && k < ncells;
-      v[k] = on ? __ldg(e0 + kx * NE + ky * sy + kz * sz + li * 28) : 0.0f;
-      pos[k] = pos0 + 2 * ((kz * R.cy + ky) * R.cx + kx);
-    }
-    for (int e = lane; e < len; e += 32) rb[e] = 0.0f;
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (k < ncells) {
-        if (col) rb[pos[k]] += v[k];
+    mrgdev::decompose(g, r0, ix, iy, iz);
+    const int64_t r1 = (r0 + GRUN < nrows) ? r0 + GRUN : nrows;
+    for (int64_t n = r0; n < r1; ++n) {
+      const mrgdev::RowInfo R = mrgdev::row_info<2>(g, ix, iy, iz);
+      const int len = R.cx * R.cy * R.cz;
+      float* row = J + R.rp;
+      if (node_fixed(g, ix, iy, iz)) {
+        const int dg = (int)(mrgdev::diag_pos(R, ix, iy, iz) - R.rp);
+        if (ovw) {
+          for (int e = lane; e < len; e += 32) __stcs(row + e, e == dg ? 1.0f : 0.0f);
+        } else if (lane == 0) {
+          row[dg] = 1.0f;
+        }
+      } else {
+        int fx, fy, fz, nxc, nyc, nzc;
+        axis_cells(ix, g.nn[0], 2, fx, nxc);
+        axis_cells(iy, g.nn[1], 2, fy, nyc);
+        axis_cells(iz, g.nn[2], 2, fz, nzc);
+        // cell (fx+kx, fy+ky, fz+kz): local row index li0 - 2 (kx + 3 ky + 9 kz), position of this lane's
+        // column in the row pos0 + 2 (kz cy cx + ky cx + kx)
+        const int li0 = (ix - 2 * fx) + 3 * (iy - 2 * fy) + 9 * (iz - 2 * fz);
+        const int pos0 = ((2 * fz + ljz - R.lz) * R.cy + (2 * fy + ljy - R.ly)) * R.cx + (2 * fx + ljx - R.lx);
+        const float* e0 = E + (fx + (int64_t)ncx * (fy + (int64_t)ncy * fz)) * NE + lane;
+        for (int e = lane; e < len; e += 32) rb[e] = 0.0f;
+        __syncwarp();
+        switch ((nxc - 1) | ((nyc - 1) << 1) | ((nzc - 1) << 2)) {
+          case 0: gather_cells<1, 1, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          case 1: gather_cells<2, 1, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          case 2: gather_cells<1, 2, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          case 3: gather_cells<2, 2, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          case 4: gather_cells<1, 1, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          case 5: gather_cells<2, 1, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          case 6: gather_cells<1, 2, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+          default: gather_cells<2, 2, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+        }
+        for (int e = lane; e < len; e += 32) {
+          if (ovw) __stcs(row + e, rb[e]); else row[e] += rb[e];
+        }
         __syncwarp();
       }
+      // next node along x (carry into y, z)
+      if (++ix == g.nn[0]) {
+        ix = 0;
+        if (++iy == g.nn[1]) { iy = 0; ++iz; }
+      }
     }
-    for (int e = lane; e < len; e += 32) {
-      if (ovw) __stcs(row + e, rb[e]); else row[e] += rb[e];
-    }
-    __syncwarp();
   }
 }
 
@@ -568,7 +589,9 @@ int mrg_q2tc_launch(const mrg_problem* p, Q2Tc* T, float* J, bool ovw, int* err,
   k_q2_elem_tc<<<grid, THREADS, SMEM_BYTES, s>>>(T->d_w, T->d_h, T->mE, T->ntiles, T->ksteps, err);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return mrg_cuda_check(e, "tensor-core element kernel launch");
-  const int64_t warps_needed = p->ndof;
+  if ((int64_t)p->g.nc[0] * p->g.nc[1] * NE * 2 >= ((int64_t)1 << 31))
+    return mrg_fail(MRG_ENOTSUP, "tensor-core Q2 path: an x-y cell plane is too large for 32-bit strides");
+  const int64_t warps_needed = (p->ndof + GRUN - 1) / GRUN;
   int64_t blocks = (warps_needed * 32 + GT - 1) / GT;
   if (blocks > (int64_t)nsm * 16) blocks = (int64_t)nsm * 16;
   k_q2_gather<<<(unsigned)blocks, GT, 0, s>>>(p->g, p->ndof, T->d_e, J, ovw ? 1 : 0);

@@ -7,7 +7,8 @@ The reference has no serving mode; this is the request loop around the GB300 pat
   estimated before admission and returned when it completes), so requests that arrive while others
   are running are admitted as soon as a slot and memory free up;
 * every slot is a host thread with its own CUDA stream; a request's whole solve (problem creation,
-  coefficient generation, Newton with PCG) is enqueued on that stream and runs inside library calls
+  coefficient generation, Newton with multigrid-preconditioned CG or BiCGStab, or Jacobi-preconditioned
+  when asked) is enqueued on that stream and runs inside library calls
   that release the GIL, so the kernels of different requests overlap on the device;
 * state (mesh, coefficients, Jacobian, vectors) stays on the device for the life of the request; the
   solution is copied to the host once, at completion;
@@ -73,17 +74,21 @@ def poisson_stream(rate=200.0, count=400, edge=(16, 96), nonlinear_fraction=0.5,
 
 
 def estimate_bytes(req: Request) -> int:
-    """Device bytes a request holds while admitted (problem data, Jacobian, Newton/PCG vectors)."""
+    """Device bytes a request holds while admitted (problem data, Jacobian, Newton / Krylov vectors and
+    the multigrid hierarchy: coarse operators ~1/7 of the fine nonzeros, six vectors per level, CG and
+    BiCGStab vectors on the fine level)."""
     n = req.n
     ndof = (n + 1) ** 3
     ncell = n ** 3
     nnz = (3 * (n + 1) - 2) ** 3
-    jbytes = nnz * (4 if req.mixed else 8)
+    w = 4 if req.mixed else 8
+    jbytes = nnz * w
     vec = ndof * 8 * 9 + (ndof * 4 * 6 if req.mixed else 0)
-    return int(jbytes + vec + ncell * (8 + 4) + 4 * 1024 * 1024)
+    hier = int(nnz * w / 7) + int(ndof * 1.15) * 6 * w + ndof * 10 * w
+    return int(jbytes + vec + hier + ncell * (8 + 4) + 4 * 1024 * 1024)
 
 
-def solve_request(req: Request, stream: torch.cuda.Stream, keep_solution=False):
+def solve_request(req: Request, stream: torch.cuda.Stream, keep_solution=False, preconditioner="gmg"):
     """Runs one request to completion on `stream`; returns (Result without timing, u on host or None)."""
     n = req.n
     t0 = time.perf_counter()
@@ -103,7 +108,7 @@ def solve_request(req: Request, stream: torch.cuda.Stream, keep_solution=False):
                 u = 0.1 * torch.rand(P.info.n_dofs, generator=gen, device="cuda", dtype=torch.float64)
             S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=30,
                               linear_tol=1e-3 if req.mixed else 1e-11, linear_maxiter=20000,
-                              mixed_precision=req.mixed)
+                              mixed_precision=req.mixed, preconditioner=preconditioner)
             stream.synchronize()
             t1 = time.perf_counter()
             res = S.nonlinearSolver(u, stream=stream, raise_on_noconv=False)
@@ -118,8 +123,9 @@ def solve_request(req: Request, stream: torch.cuda.Stream, keep_solution=False):
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes=80 * 10**9, slots=12, keep_solutions=False):
+    def __init__(self, hbm_budget_bytes=80 * 10**9, slots=12, keep_solutions=False, preconditioner="gmg"):
         self.budget = int(hbm_budget_bytes)
+        self.preconditioner = preconditioner
         self.slots = slots
         self.keep = keep_solutions
         self._lock = threading.Condition()
@@ -130,6 +136,7 @@ class Server:
         self.peak_bytes = 0
         self.peak_active = 0
         self._active = 0
+        self.errors: list[tuple[int, str]] = []  # (request id, exception) of requests that failed outside the library
 
     # admission: FIFO head may start when a slot is free and its bytes fit in the budget
     def _take(self):
@@ -170,10 +177,13 @@ class Server:
                                            0, 0, float("nan"), L.MRG_ENOMEM, 0.0))
                 continue
             try:
-                res, uh, chk, dofs = solve_request(req, stream, self.keep)
+                res, uh, chk, dofs = solve_request(req, stream, self.keep, self.preconditioner)
                 status = res.status
             except L.MrgError as e:
                 res, uh, chk, dofs, status = None, None, 0.0, 0, e.status
+            except Exception as e:  # anything else fails this request alone, never the worker
+                self.errors.append((req.rid, repr(e)))
+                res, uh, chk, dofs, status = None, None, 0.0, 0, L.MRG_EINVAL
             finally:
                 self._release(need)
             end = time.perf_counter() - t0

@@ -32,7 +32,8 @@ def _result(st: L.SolveStats) -> SolveResult:
 
 class SolverManager:
     def __init__(self, problem: Problem, nonlinear_tol=1.0e-6, max_nonlinear_iters=10, linear_tol=1.0e-7,
-                 linear_maxiter=100000, mixed_precision=False, reuse_jacobian=False, krylov="auto"):
+                 linear_maxiter=100000, mixed_precision=False, reuse_jacobian=False, krylov="auto",
+                 preconditioner="jacobi"):
         self.problem = problem
         self.NLtol = nonlinear_tol
         self.maxNLiter = max_nonlinear_iters
@@ -41,6 +42,12 @@ class SolverManager:
         self.mixed = mixed_precision
         self.reuse_jacobian = reuse_jacobian
         self.krylov = {"auto": L.MRG_KRYLOV_AUTO, "pcg": L.MRG_KRYLOV_PCG, "bicgstab": L.MRG_KRYLOV_BICGSTAB}[krylov]
+        # "jacobi": the reference's SolverManager::PCG; "gmg": geometric multigrid V-cycle (Q1 only), the
+        # structured-grid counterpart of the reference's Belos + MueLu option.  The choice is a property
+        # of the problem handle (mrg_set_preconditioner) and applies to PCG and to Newton's CG.
+        self.preconditioner = preconditioner
+        prec = {"jacobi": L.MRG_PREC_JACOBI, "gmg": L.MRG_PREC_GMG}[preconditioner]
+        L.check(L.lib().mrg_set_preconditioner(problem.handle, prec), "mrg_set_preconditioner")
 
     def setDirichlet(self, u: torch.Tensor, stream=None):
         _require_cuda(u, "u", torch.float64, self.problem.info.n_dofs)
@@ -57,7 +64,8 @@ class SolverManager:
 
     def PCG(self, J: torch.Tensor, b: torch.Tensor, x: torch.Tensor, tol: float, maxiter: int, stream=None,
             raise_on_noconv=True) -> SolveResult:
-        """Jacobi PCG on J x = b; x holds the initial guess and receives the solution."""
+        """Preconditioned CG on J x = b (Jacobi, or multigrid when chosen); x holds the initial guess and
+        receives the solution."""
         info = self.problem.info
         fp32 = J.dtype == torch.float32
         _require_cuda(J, "J", None, info.nnz)

@@ -16,7 +16,7 @@ class FakeSolve:
         self.lock = threading.Lock()
         self.fail_ids = set(fail_ids)
 
-    def __call__(self, req, stream, keep):
+    def __call__(self, req, stream, keep, preconditioner="gmg"):
         with self.lock:
             self.active += 1
             self.peak = max(self.peak, self.active)
@@ -89,3 +89,22 @@ def test_poisson_stream_shape():
     assert 180 < rate < 220
     frac = sum(r.kind == "nonlinear" for r in reqs) / len(reqs)
     assert 0.45 < frac < 0.55
+
+
+def test_unexpected_exception_fails_only_that_request(monkeypatch):
+    """A request whose solve raises something other than MrgError is reported failed; the worker and the
+    other requests carry on."""
+    class Boom(FakeSolve):
+        def __call__(self, req, stream, keep, preconditioner="gmg"):
+            if req.rid == 2:
+                raise RuntimeError("injected")
+            return super().__call__(req, stream, keep, preconditioner)
+
+    f = Boom()
+    monkeypatch.setattr(serving, "solve_request", f)
+    monkeypatch.setattr(serving.torch.cuda, "Stream", lambda: None)
+    reqs = serving.poisson_stream(rate=1000.0, count=6, edge=(4, 6), seed=2)
+    srv = serving.Server(hbm_budget_bytes=10**12, slots=2)
+    out = srv.run(reqs, realtime=False)
+    assert out["requests"] == 6 and out["ok"] == 5
+    assert [rid for rid, _ in srv.errors] == [2]
