@@ -93,10 +93,42 @@ struct GScal {
   int err;
 };
 
-template <typename T>
+template <int P, typename T>
 __device__ __forceinline__ auto row_prod(const Grid& g, const RowInfo& R, const T* vals, const T* x) {
-  if constexpr (sizeof(T) == 4) return row_apply_f<1>(g, R, vals, x);
-  else return row_apply<1, double, double>(g, R, vals, x);
+  if constexpr (sizeof(T) == 4) return row_apply_f<P>(g, R, vals, x);
+  else return row_apply<P, double, double>(g, R, vals, x);
+}
+
+// f(n, R, vals) for every row: Q1 rows through the per-warp staged loop, Q2 rows (125-point) read directly.
+template <int P, typename T, typename F>
+__device__ __forceinline__ bool level_rows(const Grid& g, int64_t n, const T* __restrict__ A, unsigned char* smem_raw,
+                                           uint64_t* mbar, F&& f) {
+  if constexpr (P == 1) {
+    return warp_staged_rows<T>(g, n, A, smem_raw, mbar, f);
+  } else {
+    for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+      int ix, iy, iz;
+      decompose(g, i, ix, iy, iz);
+      const RowInfo R = row_info<P>(g, ix, iy, iz);
+      f(i, R, A + R.rp);
+    }
+    return true;
+  }
+}
+
+// Per-axis polynomial order of a grid's coupling ranges (an intermediate grid of the Q2 -> Q1 Galerkin
+// sweeps couples +-1 along the swept axes and +-2 along the others).
+struct P3 {
+  int p[3];
+};
+
+__device__ __forceinline__ RowInfo row_info_p3(const Grid& g, const P3& pp, int ix, int iy, int iz) {
+  RowInfo R;
+  axis_range(ix, g.nn[0], pp.p[0], R.lx, R.cx);
+  axis_range(iy, g.nn[1], pp.p[1], R.ly, R.cy);
+  if (g.dim == 3) axis_range(iz, g.nn[2], pp.p[2], R.lz, R.cz); else { R.lz = 0; R.cz = 1; }
+  R.rp = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)R.cz * (g.P[1][iy] * g.T[0] + (int64_t)R.cy * g.P[0][ix]);
+  return R;
 }
 
 __device__ __forceinline__ bool is_done(const GScal* S) { return ((volatile const GScal*)S)->done != 0; }
@@ -108,14 +140,14 @@ __device__ __forceinline__ bool is_done(const GScal* S) { return ((volatile cons
 // each keeping the 27-point layout on an intermediate grid: ~160 multiply-adds per output row instead
 // of ~5,800 for the direct triple product.
 template <typename T>
-__global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, Grid gc, int axis, const T* __restrict__ Af,
+__global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, P3 pf, Grid gc, P3 pc, int axis, const T* __restrict__ Af,
                                                  T* __restrict__ Ac, int* __restrict__ err) {
   const int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x;
   const int64_t nrows = (int64_t)gc.nn[0] * gc.nn[1] * gc.nn[2];
   if (n >= nrows) return;
   int I[3];
   decompose(gc, n, I[0], I[1], I[2]);
-  const RowInfo Rc = row_info<1>(gc, I[0], I[1], I[2]);
+  const RowInfo Rc = row_info_p3(gc, pc, I[0], I[1], I[2]);
   const int lenc = Rc.cx * Rc.cy * Rc.cz;
   T* out = Ac + Rc.rp;
   if (node_fixed(gc, I[0], I[1], I[2])) {
@@ -123,9 +155,10 @@ __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, Grid gc, int axis, con
     for (int e = 0; e < lenc; ++e) out[e] = (e == dg) ? T(1) : T(0);
     return;
   }
-  T acc[27];
-#pragma unroll
-  for (int e = 0; e < 27; ++e) acc[e] = T(0);
+  constexpr int MAXROW = 75;  // 3 x 5 x 5: the widest output row (one axis swept from a Q2 grid)
+  if (lenc > MAXROW) { atomicExch(err, 1); return; }
+  T acc[MAXROW];
+  for (int e = 0; e < lenc; ++e) acc[e] = T(0);
   int ci[3];
   float cw[3];
   const int nci = axis_children(I[axis], gf.nn[axis], gc.nn[axis], 1, ci, cw);
@@ -133,7 +166,7 @@ __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, Grid gc, int axis, con
     int f[3] = {I[0], I[1], I[2]};
     f[axis] = ci[c];
     if (node_fixed(gf, f[0], f[1], f[2])) continue;
-    const RowInfo Rf = row_info<1>(gf, f[0], f[1], f[2]);
+    const RowInfo Rf = row_info_p3(gf, pf, f[0], f[1], f[2]);
     const T* vals = Af + Rf.rp;
     int e = 0;
     for (int jz = Rf.lz; jz < Rf.lz + Rf.cz; ++jz)
@@ -158,7 +191,7 @@ __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, Grid gc, int axis, con
 }
 
 // minv = 1 / diag; Gershgorin bound max_i sum_j |a_ij| / |a_ii| into lmax (as float bits, atomicMax)
-template <typename T>
+template <int P, typename T>
 __global__ void __launch_bounds__(NT) k_diag(Grid g, const T* __restrict__ A, T* __restrict__ minv,
                                              unsigned int* __restrict__ lmax_bits) {
   const int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x;
@@ -167,7 +200,7 @@ __global__ void __launch_bounds__(NT) k_diag(Grid g, const T* __restrict__ A, T*
   if (n < nrows) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
-    const RowInfo R = row_info<1>(g, ix, iy, iz);
+    const RowInfo R = row_info<P>(g, ix, iy, iz);
     const T* vals = A + R.rp;
     const int len = R.cx * R.cy * R.cz;
     const T dgv = vals[diag_pos(R, ix, iy, iz) - R.rp];
@@ -238,7 +271,7 @@ __global__ void __launch_bounds__(NT) k_coarse_inv(Grid g, const T* __restrict__
 // ---- cycle kernels --------------------------------------------------------------------------------
 // Chebyshev step `k` (0..NU-1): d = rho_k rho_{k-1} d + (2 rho_k / delta) D^{-1}(b - A x)  (k = 0:
 // d = D^{-1}(b - A x) / theta); xout = x + d.  zero_x: x = 0 (no SpMV).
-template <typename T>
+template <int P, typename T>
 __global__ void __launch_bounds__(NT) k_cheb(LevDev<T> L, const T* __restrict__ xin, T* __restrict__ xout, int k,
                                              int zero_x, const unsigned int* __restrict__ lmax_bits,
                                              const GScal* __restrict__ S, int* __restrict__ err) {
@@ -264,21 +297,21 @@ __global__ void __launch_bounds__(NT) k_cheb(LevDev<T> L, const T* __restrict__ 
     for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < L.n; n += (int64_t)gridDim.x * NT) fin(n, T(0));
     return;
   }
-  const bool ok = warp_staged_rows<T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
-    fin(n, (T)row_prod<T>(L.g, R, vals, xin));
+  const bool ok = level_rows<P, T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
+    fin(n, (T)row_prod<P, T>(L.g, R, vals, xin));
   });
   if (!ok) atomicExch(err, 3);
 }
 
 // r = b - A x
-template <typename T>
+template <int P, typename T>
 __global__ void __launch_bounds__(NT) k_resid(LevDev<T> L, const T* __restrict__ x, const GScal* __restrict__ S,
                                               int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
   if (is_done(S)) return;
-  const bool ok = warp_staged_rows<T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
-    L.r[n] = L.b[n] - (T)row_prod<T>(L.g, R, vals, x);
+  const bool ok = level_rows<P, T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
+    L.r[n] = L.b[n] - (T)row_prod<P, T>(L.g, R, vals, x);
   });
   if (!ok) atomicExch(err, 3);
 }
@@ -413,15 +446,15 @@ __global__ void __launch_bounds__(NT) k_cg_rz(int64_t n, CgVec<T> V, int first) 
 }
 
 // w = A z ; p = z + beta p ; q = w + beta q ; partial p.q ; alpha = rho / p.q
-template <typename T>
+template <int P, typename T>
 __global__ void __launch_bounds__(NT) k_cg_spmv(Grid g, int64_t n, const T* __restrict__ A, CgVec<T> V) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
   if (is_done(V.S)) return;
   const T beta = (T)V.S->beta;
   double pq = 0.0;
-  const bool ok = warp_staged_rows<T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
-    const T w = (T)row_prod<T>(g, R, vals, V.z);
+  const bool ok = level_rows<P, T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
+    const T w = (T)row_prod<P, T>(g, R, vals, V.z);
     const T pn = V.z[i] + beta * V.p[i];
     const T qn = w + beta * V.q[i];
     V.p[i] = pn;
@@ -526,7 +559,7 @@ __global__ void __launch_bounds__(NT) k_bg_p(int64_t n, BgVec<T> V) {
 }
 
 // STEP 0: v = A ph, rv = rh . v, alpha = rho / rv.   STEP 1: t = A sh, omega = (t . s) / (t . t).
-template <typename T, int STEP>
+template <int P, typename T, int STEP>
 __global__ void __launch_bounds__(NT) k_bg_spmv(Grid g, int64_t n, const T* __restrict__ A, BgVec<T> V) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
@@ -534,8 +567,8 @@ __global__ void __launch_bounds__(NT) k_bg_spmv(Grid g, int64_t n, const T* __re
   const T* in = STEP == 0 ? V.ph : V.sh;
   T* out = STEP == 0 ? V.v : V.t;
   double d0 = 0.0, d1 = 0.0;
-  const bool ok = warp_staged_rows<T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
-    const T y = (T)row_prod<T>(g, R, vals, in);
+  const bool ok = level_rows<P, T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
+    const T y = (T)row_prod<P, T>(g, R, vals, in);
     out[i] = y;
     if (STEP == 0) {
       d0 += (double)V.rh[i] * (double)y;
@@ -627,9 +660,11 @@ struct HLevel {
   Grid g;
   int64_t n = 0, nnz = 0;
   Xfer X{{0, 0, 0}};          // how this level was coarsened from the finer one
+  P3 pp{{1, 1, 1}};           // per-axis coupling order of this level (2 only on a Q2 level 0)
   int nsweep = 0;             // Galerkin sweeps from the finer level (one per coarsened axis)
   int sweep_axis[3] = {0, 0, 0};
   Grid mid[2];                // intermediate grids after all but the last sweep
+  P3 mid_pp[2];
   int64_t* d_mid_pref[2] = {nullptr, nullptr};
   int64_t* d_pref = nullptr;  // prefix tables (coarse levels)
   void* A = nullptr;          // coarse levels: owned; level 0: the caller's Jacobian
@@ -669,12 +704,12 @@ GmgData* gdata(mrg_problem* p) {
 }
 
 // Host grid of a p = 1 level with nn nodes per axis (prefix tables uploaded to d_pref).
-int make_level_grid(const Grid& fine, const int nn[3], cudaStream_t s, Grid& g, int64_t*& d_pref) {
+int make_level_grid(const Grid& fine, const int nn[3], const P3& pp, cudaStream_t s, Grid& g, int64_t*& d_pref) {
   g = fine;
-  g.p = 1;
+  g.p = std::max(pp.p[0], std::max(pp.p[1], pp.p[2]));
   for (int k = 0; k < 3; ++k) {
     g.nn[k] = nn[k];
-    g.nc[k] = (k < fine.dim) ? nn[k] - 1 : 1;
+    g.nc[k] = (k < fine.dim) ? (nn[k] - 1) / pp.p[k] : 1;
   }
   std::vector<int64_t> pref;
   int64_t offs[3];
@@ -684,7 +719,7 @@ int make_level_grid(const Grid& fine, const int nn[3], cudaStream_t s, Grid& g, 
     pref.push_back(0);
     for (int i = 0; i < g.nn[k]; ++i) {
       int lo, cnt;
-      if (k < g.dim) axis_range(i, g.nn[k], 1, lo, cnt); else cnt = 1;
+      if (k < g.dim) axis_range(i, g.nn[k], pp.p[k], lo, cnt); else cnt = 1;
       acc += cnt;
       pref.push_back(acc);
     }
@@ -735,18 +770,21 @@ int build_hier(const mrg_problem* p, Hier<T>*& out, cudaStream_t s) {
   L0.g = p->g;
   L0.n = p->ndof;
   L0.nnz = p->nnz;
+  for (int k = 0; k < 3; ++k) L0.pp.p[k] = (k < p->g.dim) ? p->g.p : 1;
   H->L.push_back(L0);
   // cell size per axis (box estimate); an axis is coarsened only while its cells are at most twice as
   // long as the shortest ones (semi-coarsening keeps point smoothing effective on stretched grids)
   double h[3] = {p->h[0], p->h[1], p->h[2]};
   while ((int)H->L.size() < MAXLEV) {
     const Grid& gf = H->L.back().g;
+    const P3 pf = H->L.back().pp;
+    const bool ptransfer = pf.p[0] == 2;  // Q2 level 0 -> Q1 on the same cells: every axis, h unchanged
     int nn[3], co[3] = {0, 0, 0}, any = 0;
     double hmin = 1e300;
     for (int k = 0; k < gf.dim; ++k) hmin = std::fmin(hmin, h[k]);
     for (int pass = 0; pass < 2 && !any; ++pass)
       for (int k = 0; k < gf.dim; ++k)
-        if (gf.nn[k] - 1 >= 3 && (pass == 1 || h[k] <= 2.0 * hmin * (1.0 + 1e-9))) {
+        if (ptransfer || (gf.nn[k] - 1 >= 3 && (pass == 1 || h[k] <= 2.0 * hmin * (1.0 + 1e-9)))) {
           co[k] = 1;
           any = 1;
         }
@@ -754,22 +792,26 @@ int build_hier(const mrg_problem* p, Hier<T>*& out, cudaStream_t s) {
       nn[k] = gf.nn[k];
       if (co[k]) {
         nn[k] = (gf.nn[k] - 1 + 1) / 2 + 1;
-        h[k] *= 2.0;
+        if (!ptransfer) h[k] *= 2.0;
       }
     }
     const int64_t nfine = H->L.back().n;
-    if (!any || nfine <= MAXC) break;
+    if (!any || (nfine <= MAXC && !ptransfer)) break;
     HLevel Lc;
-    int rc = make_level_grid(gf, nn, s, Lc.g, Lc.d_pref);
+    int rc = make_level_grid(gf, nn, Lc.pp, s, Lc.g, Lc.d_pref);
     if (rc) { H->L.push_back(Lc); return fail(rc); }
     for (int k = 0; k < 3; ++k) Lc.X.co[k] = co[k];
-    // sweep plan: coarsen the axes one at a time; intermediate grids for all but the last sweep
+    // sweep plan: coarsen the axes one at a time; intermediate grids for all but the last sweep (a
+    // swept axis couples at order 1, the others keep the finer level's order)
     int cur[3] = {gf.nn[0], gf.nn[1], gf.nn[2]};
+    P3 cp = pf;
     for (int k = 0; k < 3; ++k)
       if (co[k]) Lc.sweep_axis[Lc.nsweep++] = k;
     for (int w = 0; w + 1 < Lc.nsweep; ++w) {
       cur[Lc.sweep_axis[w]] = nn[Lc.sweep_axis[w]];
-      rc = make_level_grid(gf, cur, s, Lc.mid[w], Lc.d_mid_pref[w]);
+      cp.p[Lc.sweep_axis[w]] = 1;
+      Lc.mid_pp[w] = cp;
+      rc = make_level_grid(gf, cur, cp, s, Lc.mid[w], Lc.d_mid_pref[w]);
       if (rc) { H->L.push_back(Lc); return fail(rc); }
     }
     Lc.n = (int64_t)nn[0] * nn[1] * nn[2];
@@ -822,11 +864,11 @@ int set_staged_attr() {
   static cudaError_t e = cudaSuccess;
   std::call_once(once, [] {
     const int smem = (NT / 32) * 2 * wbuf_elems<T>() * (int)sizeof(T);
-    e = cudaFuncSetAttribute(k_cheb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cg_spmv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bg_spmv<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bg_spmv<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = cudaFuncSetAttribute(k_cheb<1, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resid<1, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cg_spmv<1, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bg_spmv<1, T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bg_spmv<1, T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   });
   return e == cudaSuccess ? MRG_OK : mrg_cuda_check(e, "multigrid smem attribute");
 }
@@ -846,24 +888,47 @@ int setup_values(Hier<T>* H, const T* J, cudaStream_t s) {
     if (l > 0) {
       const HLevel& F = H->L[l - 1];
       const Grid* gin = &F.g;
+      P3 pin = F.pp;
       const T* ain = (const T*)F.A;
       for (int w = 0; w < L.nsweep; ++w) {
         const bool last = (w + 1 == L.nsweep);
         const Grid& gout = last ? L.g : L.mid[w];
+        const P3 pout = last ? L.pp : L.mid_pp[w];
         T* aout = last ? (T*)L.A : H->mid[w];
         const int64_t nout = (int64_t)gout.nn[0] * gout.nn[1] * gout.nn[2];
-        k_rap_axis<T><<<nblk(nout, NT), NT, 0, s>>>(*gin, gout, L.sweep_axis[w], ain, aout, H->err);
+        k_rap_axis<T><<<nblk(nout, NT), NT, 0, s>>>(*gin, pin, gout, pout, L.sweep_axis[w], ain, aout, H->err);
         MRG_CUDA(cudaGetLastError());
         gin = &gout;
+        pin = pout;
         ain = aout;
       }
     }
-    k_diag<T><<<nblk(L.n, NT), NT, 0, s>>>(L.g, (const T*)L.A, (T*)L.minv, H->lmax + l);
+    if (L.pp.p[0] == 2) k_diag<2, T><<<nblk(L.n, NT), NT, 0, s>>>(L.g, (const T*)L.A, (T*)L.minv, H->lmax + l);
+    else k_diag<1, T><<<nblk(L.n, NT), NT, 0, s>>>(L.g, (const T*)L.A, (T*)L.minv, H->lmax + l);
     MRG_CUDA(cudaGetLastError());
   }
   k_coarse_inv<T><<<1, NT, 0, s>>>(H->L.back().g, (const T*)H->L.back().A, H->cinv, H->err);
   MRG_CUDA(cudaGetLastError());
   return MRG_OK;
+}
+
+// Launches of the row kernels for a level: Q1 levels use the staged loop (dynamic shared memory, fewer
+// CTAs per SM), a Q2 level 0 the direct row loop.
+template <typename T>
+void launch_cheb(const HLevel& L, const LevDev<T>& D, const T* xin, T* xout, int k, int zero_x,
+                 const unsigned int* lmax, const GScal* S, int* err, cudaStream_t s) {
+  if (zero_x)
+    k_cheb<1, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, xin, xout, k, 1, lmax, S, err);
+  else if (L.pp.p[0] == 2)
+    k_cheb<2, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, xin, xout, k, 0, lmax, S, err);
+  else
+    k_cheb<1, T><<<grid_for(D.n, staged_per_sm<T>()), NT, staged_smem<T>(), s>>>(D, xin, xout, k, 0, lmax, S, err);
+}
+
+template <typename T>
+void launch_resid(const HLevel& L, const LevDev<T>& D, const T* x, const GScal* S, int* err, cudaStream_t s) {
+  if (L.pp.p[0] == 2) k_resid<2, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, x, S, err);
+  else k_resid<1, T><<<grid_for(D.n, staged_per_sm<T>()), NT, staged_smem<T>(), s>>>(D, x, S, err);
 }
 
 // One V(NU, NU) cycle: out = M^{-1} in on level 0 (in, out: level-0 vectors not used by the cycle).
@@ -874,11 +939,10 @@ void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
   for (int l = 0; l < nl - 1; ++l) {
     LevDev<T> D = levdev<T>(H->L[l]);
     if (l == 0) D.b = const_cast<T*>(in);
-    const unsigned gs = grid_for(D.n, staged_per_sm<T>()), ge = grid_for(D.n, 16);
     // pre-smoothing from x = 0: xa <- step 0, xb <- step 1
-    k_cheb<T><<<ge, NT, 0, s>>>(D, D.xa, D.xa, 0, 1, H->lmax + l, S, H->err);
-    k_cheb<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xa, D.xb, 1, 0, H->lmax + l, S, H->err);
-    k_resid<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xb, S, H->err);
+    launch_cheb<T>(H->L[l], D, D.xa, D.xa, 0, 1, H->lmax + l, S, H->err, s);
+    launch_cheb<T>(H->L[l], D, D.xa, D.xb, 1, 0, H->lmax + l, S, H->err, s);
+    launch_resid<T>(H->L[l], D, D.xb, S, H->err, s);
     const HLevel& C = H->L[l + 1];
     k_restrict<T><<<grid_for(C.n, 16), NT, 0, s>>>(D.g, C.g, C.X, D.r, (T*)C.b, S);
   }
@@ -888,11 +952,10 @@ void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
     LevDev<T> D = levdev<T>(H->L[l]);
     if (l == 0) D.b = const_cast<T*>(in);
     const HLevel& C = H->L[l + 1];
-    const unsigned gs = grid_for(D.n, staged_per_sm<T>());
     k_prolong<T><<<grid_for(D.n, 16), NT, 0, s>>>(D.g, C.g, C.X, (const T*)C.xb, D.xb, S);
     // post-smoothing: xb -> xa (step 0), xa -> xb (step 1; level 0: -> out)
-    k_cheb<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xb, D.xa, 0, 0, H->lmax + l, S, H->err);
-    k_cheb<T><<<gs, NT, staged_smem<T>(), s>>>(D, D.xa, l == 0 ? out : D.xb, 1, 0, H->lmax + l, S, H->err);
+    launch_cheb<T>(H->L[l], D, D.xb, D.xa, 0, 0, H->lmax + l, S, H->err, s);
+    launch_cheb<T>(H->L[l], D, D.xa, l == 0 ? out : D.xb, 1, 0, H->lmax + l, S, H->err, s);
   }
 }
 
@@ -907,7 +970,8 @@ void enqueue_iters(Hier<T>* H, int count, cudaStream_t s) {
   CgVec<T> V = cgvec(H);
   const unsigned ge = grid_for(L0.n, 16), gs = grid_for(L0.n, staged_per_sm<T>());
   for (int it = 0; it < count; ++it) {
-    k_cg_spmv<T><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    if (L0.pp.p[0] == 2) k_cg_spmv<2, T><<<ge, NT, 0, s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    else k_cg_spmv<1, T><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
     k_cg_update<T><<<ge, NT, 0, s>>>(L0.n, V);
     enqueue_vcycle(H, H->r, (T*)H->L[0].xb, s);
     k_cg_rz<T><<<ge, NT, 0, s>>>(L0.n, V, 0);
@@ -1003,10 +1067,12 @@ void enqueue_bg_iters(Hier<T>* H, int count, cudaStream_t s) {
   for (int it = 0; it < count; ++it) {
     k_bg_p<T><<<ge, NT, 0, s>>>(L0.n, V);
     enqueue_vcycle(H, H->p, H->ph, s);
-    k_bg_spmv<T, 0><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    if (L0.pp.p[0] == 2) k_bg_spmv<2, T, 0><<<ge, NT, 0, s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    else k_bg_spmv<1, T, 0><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
     k_bg_s<T><<<ge, NT, 0, s>>>(L0.n, V);
     enqueue_vcycle(H, H->sv, H->sh, s);
-    k_bg_spmv<T, 1><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    if (L0.pp.p[0] == 2) k_bg_spmv<2, T, 1><<<ge, NT, 0, s>>>(L0.g, L0.n, (const T*)L0.A, V);
+    else k_bg_spmv<1, T, 1><<<gs, NT, staged_smem<T>(), s>>>(L0.g, L0.n, (const T*)L0.A, V);
     k_bg_update<T><<<ge, NT, 0, s>>>(L0.n, V);
   }
 }
@@ -1070,7 +1136,7 @@ void mrg_gmg_free(mrg_problem* p) {
 // solution.
 int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
                   mrg_solve_stats* st, cudaStream_t s) {
-  if (p->g.p != 1) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 problems only");
+  if (p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 and Q2 problems only");
   GmgData* G = gdata(p);
   int rc;
   if (fp32) {
@@ -1084,7 +1150,7 @@ int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, dou
 // Same for a nonsymmetric J: right-preconditioned BiCGStab with the multigrid V-cycle.
 int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
                      mrg_solve_stats* st, cudaStream_t s) {
-  if (p->g.p != 1) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 problems only");
+  if (p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 and Q2 problems only");
   GmgData* G = gdata(p);
   int rc;
   if (fp32) {
@@ -1099,7 +1165,7 @@ extern "C" int mrg_set_preconditioner(mrg_problem* p, int32_t kind) {
   if (!p) return mrg_fail(MRG_EINVAL, "mrg_set_preconditioner: null problem");
   if (kind != MRG_PREC_JACOBI && kind != MRG_PREC_GMG)
     return mrg_fail(MRG_EINVAL, "mrg_set_preconditioner: unknown preconditioner");
-  if (kind == MRG_PREC_GMG && p->g.p != 1) return mrg_fail(MRG_ENOTSUP, "multigrid preconditioner: Q1 problems only");
+  if (kind == MRG_PREC_GMG && p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid preconditioner: Q1 and Q2 problems only");
   gdata(p)->kind = kind;
   return MRG_OK;
 }

@@ -78,13 +78,41 @@ def test_gmg_pcg_is_deterministic_and_warm_restartable(cuda):
 
 
 @pytest.mark.gpu
-def test_gmg_rejected_for_q2(cuda):
-    from mrhyde_gb300 import SolverManager
-    from mrhyde_gb300._lib import MrgError
+@pytest.mark.parametrize("fp32", [False, True])
+def test_q2_pmultigrid_pcg_matches_oracle(cuda, fp32):
+    """Q2: the first level is the p-transfer to Q1 on the same cells, then the Q1 hierarchy."""
+    from mrhyde_gb300 import AssemblyManager, SolverManager
 
-    G = gpu_problem(dict(dim=3, order=2, n=(2, 2, 2), dirichlet_faces=1))
-    with pytest.raises(MrgError):
-        SolverManager(G, preconditioner="gmg")
+    c = _with_kappa(dict(dim=3, order=2, n=(8, 6, 5), dirichlet_faces=3), 12)
+    G, O = gpu_problem(c), oracle_problem(c)
+    A, S = AssemblyManager(G), SolverManager(G, preconditioner="gmg")
+    r, J = G.new_vector(), G.new_matrix_values(fp32=fp32)
+    A.assembleJacRes(G.new_vector(), r, J, fp32_jacobian=fp32, overwrite=True, tensor_cores=False)
+    x = G.new_vector()
+    tol = 1e-5 if fp32 else 1e-11
+    res = S.PCG(J, r, x, tol=tol, maxiter=200)
+    assert res.rel_residual <= tol and res.iterations <= (12 if fp32 else 25), res.iterations
+    ro, Jo = O.assemble(np.zeros(O.ndof))
+    xo, _, _ = O.pcg(Jo, ro, tol=1e-13, maxiter=100000)
+    np.testing.assert_allclose(x.cpu().numpy(), xo, rtol=0, atol=(3e-4 if fp32 else 1e-9) * np.abs(xo).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [False, True])
+def test_q2_nonlinear_newton_with_pmultigrid(cuda, mixed):
+    """C3's form on a small grid: Newton with p-multigrid BiCGStab zeroes the oracle's FP64 residual."""
+    from mrhyde_gb300 import SolverManager
+
+    cfg = dict(dim=3, order=2, n=(6, 5, 4), kind="diffusion_1pu2", dirichlet_faces=3, source=("const", 10.0, 0.0))
+    G, O = gpu_problem(cfg), oracle_problem(cfg)
+    S = SolverManager(G, nonlinear_tol=1e-10, max_nonlinear_iters=20, linear_tol=1e-11 if not mixed else 1e-4,
+                      mixed_precision=mixed, preconditioner="gmg")
+    u = G.new_vector()
+    res = S.nonlinearSolver(u)
+    assert res.rel_residual < 1e-10
+    r0, _ = O.assemble(O.set_dirichlet(np.zeros(O.ndof)), jac=False)
+    r, _ = O.assemble(u.cpu().numpy(), jac=False)
+    assert np.abs(r).max() <= 1e-9 * np.abs(r0).max()
 
 
 @pytest.mark.gpu
