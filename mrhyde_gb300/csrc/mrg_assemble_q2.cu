@@ -384,7 +384,10 @@ struct TPData {
   float* d_tab32 = nullptr;
   void* d_qbuf = nullptr;  // ncell * 4 NL (FP64 or FP32, by the last Jacobian request)
   size_t qbuf_bytes = 0;
-  int* d_err = nullptr;    // tensor-core kernel status (bounded waits)
+  int* d_err = nullptr;    // tensor-core kernel status (bounded waits), sticky until reported
+  int* h_err = nullptr;    // pinned mirror, refreshed asynchronously after every tensor-core launch
+  cudaEvent_t err_ev = nullptr;  // recorded after the refresh
+  bool err_pending = false;
   std::vector<double> tab_host;  // [G_x | G_y | G_z | Phi] rows of TS doubles
   Q2Tc* tc = nullptr;      // tensor-core element-matrix plan (Q2, FP32 Jacobian), built on first use
 };
@@ -461,6 +464,8 @@ void mrg_q2_free(mrg_problem* p) {
   cudaFreeAsync(Q->d_tab64, p->stream);
   cudaFreeAsync(Q->d_tab32, p->stream);
   cudaFreeAsync(Q->d_err, p->stream);
+  if (Q->err_ev) cudaEventDestroy(Q->err_ev);
+  if (Q->h_err) cudaFreeHost(Q->h_err);
   if (Q->d_qbuf) cudaFreeAsync(Q->d_qbuf, p->stream);
   mrg_q2tc_free(Q->tc, p->stream);
   delete Q;
@@ -523,21 +528,41 @@ int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t 
   void* qbuf = nullptr;
   const bool tc = doJ && P == 2 && fp32 && !(flags & MRG_ASM_CUDA_CORES);
   if (tc) {
-    // tensor cores: the residual pass writes the TF32 hi/lo planes of W straight into the plan's buffer
+    // A time-out inside a previous tensor-core launch is reported here, without synchronising: the
+    // status word is copied to pinned memory behind an event after every launch and read once that
+    // event has completed, so the assembly stays free of host synchronisation (graph-capturable once
+    // the workspace exists).
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    MRG_CUDA(cudaStreamIsCapturing(s, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    if (!capturing && Q->err_pending && cudaEventQuery(Q->err_ev) == cudaSuccess) {
+      Q->err_pending = false;
+      if (*Q->h_err) {
+        *Q->h_err = 0;
+        MRG_CUDA(cudaMemsetAsync(Q->d_err, 0, sizeof(int), s));
+        return mrg_fail(MRG_ETIMEOUT, "tensor-core element kernel: an mbarrier wait timed out in a previous launch");
+      }
+    }
+    // tensor cores: the residual pass writes the TF32 hi/lo planes of W straight into the plan's buffer.
+    // The first call allocates the workspace (element matrices, operand images) and uploads the
+    // constant operand: make it outside stream capture.
     if (!Q->tc) {
       int st = mrg_q2tc_create(p, Q->tab_host.data(), Q->T.s, &Q->tc, s);
       if (st) return st;
+      MRG_CUDA(cudaMallocHost(&Q->h_err, sizeof(int)));
+      *Q->h_err = 0;
+      MRG_CUDA(cudaEventCreateWithFlags(&Q->err_ev, cudaEventDisableTiming));
     }
     if (doR && ovw) MRG_CUDA(cudaMemsetAsync(r, 0, p->ndof * sizeof(double), s));
     int st = launch_res_t<2>(p, u, doR ? r : nullptr, mrg_q2tc_w_image(Q->tc), true, true, (doR ? 1 : 0) | 2, s);
     if (st) return st;
-    MRG_CUDA(cudaMemsetAsync(Q->d_err, 0, sizeof(int), s));
     st = mrg_q2tc_launch(p, Q->tc, (float*)J, ovw, Q->d_err, s);
     if (st) return st;
-    int herr = 0;
-    MRG_CUDA(cudaMemcpyAsync(&herr, Q->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MRG_CUDA(cudaStreamSynchronize(s));
-    if (herr) return mrg_fail(MRG_ETIMEOUT, "tensor-core element kernel: an mbarrier wait timed out");
+    MRG_CUDA(cudaMemcpyAsync(Q->h_err, Q->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!capturing) {
+      MRG_CUDA(cudaEventRecord(Q->err_ev, s));
+      Q->err_pending = true;
+    }
     return MRG_OK;
   }
   if (doJ) {

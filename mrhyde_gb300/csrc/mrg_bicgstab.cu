@@ -353,7 +353,7 @@ extern "C" int mrg_solve_bicgstab(mrg_problem* p, const void* J, int32_t fp32, c
     MRG_CUDA(cudaMallocAsync(&dx, p->ndof * sizeof(double), s));
     int rc = mrg_spmv(p, J, fp32, x, res, stream);
     if (rc == MRG_OK) rc = mrg_residual_from(p, b, res, s);
-    if (rc == MRG_OK) rc = mrg_gmg_bicgstab(p, J, fp32 != 0, res, dx, rtol, maxiter, st, s);
+    if (rc == MRG_OK) rc = mrg_gmg_bicgstab(p, J, fp32 != 0, res, dx, rtol, maxiter, st, false, s);
     if (rc == MRG_OK || rc == MRG_ENOCONV) {
       k_b_add<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, dx, x);
       cudaError_t e = cudaGetLastError();

@@ -690,6 +690,7 @@ struct Hier {
   cudaGraphExec_t bgraph = nullptr;
   const void* bgraph_A = nullptr;
   cudaStream_t bgraph_stream = nullptr;
+  const void* setup_J = nullptr;  // Jacobian of the last setup
 };
 
 struct GmgData {
@@ -1014,11 +1015,15 @@ int finish_solve(mrg_problem* p, Hier<T>* H, cudaGraphExec_t graph, double* x, d
 
 template <typename T>
 int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
-           mrg_solve_stats* st, cudaStream_t s) {
+           mrg_solve_stats* st, bool reuse, cudaStream_t s) {
   int rc = set_staged_attr<T>();
   if (rc) return rc;
-  rc = setup_values(H, J, s);
-  if (rc) return rc;
+  // the level operators are rebuilt unless the caller guarantees J is unchanged since the last setup
+  if (!reuse || H->setup_J != (const void*)J) {
+    rc = setup_values(H, J, s);
+    if (rc) return rc;
+    H->setup_J = J;
+  }
   GScal init{};
   init.tol = rtol;
   init.maxiter = maxiter;
@@ -1079,15 +1084,19 @@ void enqueue_bg_iters(Hier<T>* H, int count, cudaStream_t s) {
 
 template <typename T>
 int gmg_bicgstab(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
-                 mrg_solve_stats* st, cudaStream_t s) {
+                 mrg_solve_stats* st, bool reuse, cudaStream_t s) {
   int rc = set_staged_attr<T>();
   if (rc) return rc;
   const int64_t n = p->ndof;
   if (!H->rh)
     for (T** ptr : {&H->rh, &H->v, &H->sv, &H->t, &H->ph, &H->sh})
       if (cudaMallocAsync(ptr, n * sizeof(T), s) != cudaSuccess) return mrg_fail(MRG_ENOMEM, "multigrid BiCGStab vectors");
-  rc = setup_values(H, J, s);
-  if (rc) return rc;
+  // the level operators are rebuilt unless the caller guarantees J is unchanged since the last setup
+  if (!reuse || H->setup_J != (const void*)J) {
+    rc = setup_values(H, J, s);
+    if (rc) return rc;
+    H->setup_J = J;
+  }
   GScal init{};
   init.tol = rtol;
   init.maxiter = maxiter;
@@ -1135,30 +1144,30 @@ void mrg_gmg_free(mrg_problem* p) {
 // Solves J x = b (x0 = 0) with multigrid-preconditioned CG in the precision of J; x receives the FP64
 // solution.
 int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                  mrg_solve_stats* st, cudaStream_t s) {
+                  mrg_solve_stats* st, bool reuse_setup, cudaStream_t s) {
   if (p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 and Q2 problems only");
   GmgData* G = gdata(p);
   int rc;
   if (fp32) {
     if (!G->h32 && (rc = build_hier<float>(p, G->h32, s))) return rc;
-    return gmg_cg<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, s);
+    return gmg_cg<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, reuse_setup, s);
   }
   if (!G->h64 && (rc = build_hier<double>(p, G->h64, s))) return rc;
-  return gmg_cg<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, s);
+  return gmg_cg<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, reuse_setup, s);
 }
 
 // Same for a nonsymmetric J: right-preconditioned BiCGStab with the multigrid V-cycle.
 int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                     mrg_solve_stats* st, cudaStream_t s) {
+                     mrg_solve_stats* st, bool reuse_setup, cudaStream_t s) {
   if (p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 and Q2 problems only");
   GmgData* G = gdata(p);
   int rc;
   if (fp32) {
     if (!G->h32 && (rc = build_hier<float>(p, G->h32, s))) return rc;
-    return gmg_bicgstab<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, s);
+    return gmg_bicgstab<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, reuse_setup, s);
   }
   if (!G->h64 && (rc = build_hier<double>(p, G->h64, s))) return rc;
-  return gmg_bicgstab<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, s);
+  return gmg_bicgstab<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, reuse_setup, s);
 }
 
 extern "C" int mrg_set_preconditioner(mrg_problem* p, int32_t kind) {

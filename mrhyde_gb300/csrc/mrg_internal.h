@@ -143,10 +143,11 @@ void mrg_lagrange_1d(int p, double xi, double* l, double* dl);
 // Multigrid preconditioned CG (mrg_gmg.cu)
 int mrg_gmg_kind(const mrg_problem* p);
 void mrg_gmg_free(mrg_problem* p);
+// reuse_setup: J is unchanged since the last solve with the same pointer (skip the hierarchy setup)
 int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                  mrg_solve_stats* st, cudaStream_t s);
+                  mrg_solve_stats* st, bool reuse_setup, cudaStream_t s);
 int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                     mrg_solve_stats* st, cudaStream_t s);
+                     mrg_solve_stats* st, bool reuse_setup, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);
 int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s);  // res = b - res

@@ -666,7 +666,7 @@ extern "C" int mrg_solve_pcg(mrg_problem* p, const void* J, int32_t fp32, const 
     if (rc) return rc;
     k_b_minus<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, b, w->r);
     MRG_CUDA(cudaGetLastError());
-    rc = mrg_gmg_solve(p, J, fp32 != 0, w->r, w->z, rtol, maxiter, st, s);
+    rc = mrg_gmg_solve(p, J, fp32 != 0, w->r, w->z, rtol, maxiter, st, false, s);
     if (rc && rc != MRG_ENOCONV) return rc;
     k_axpy<<<nblk(p->ndof, 256), 256, 0, s>>>(p->ndof, 1.0, w->z, x);
     MRG_CUDA(cudaGetLastError());
@@ -755,7 +755,11 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
       proceed = false;
     }
     if (solve) {
-      if (!have_J || !o->reuse_jacobian) {
+      // The thermal form is linear in u (kappa and any weak-Dirichlet face terms do not depend on u), so
+      // its Jacobian is the same at every Newton step of this call: assemble it once.  The 1+u^2 form is
+      // re-assembled every step unless reuse_jacobian asks otherwise.
+      const bool fresh = !have_J || (!o->reuse_jacobian && p->kind != MRG_THERMAL);
+      if (fresh) {
         rc = mrg_assemble(p, u, nullptr, J, jflags, stream);
         if (rc) return rc;
         have_J = true;
@@ -764,8 +768,8 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
       // the 1+u^2 Jacobian is nonsymmetric (2 u phi_j grad u . grad phi_i): BiCGStab; CG otherwise
       const bool bicg = (o->krylov == MRG_KRYLOV_BICGSTAB) || (o->krylov == MRG_KRYLOV_AUTO && p->kind != MRG_THERMAL);
       if (mrg_gmg_kind(p) == MRG_PREC_GMG) {
-        rc = bicg ? mrg_gmg_bicgstab(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s)
-                  : mrg_gmg_solve(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s);
+        rc = bicg ? mrg_gmg_bicgstab(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, !fresh, s)
+                  : mrg_gmg_solve(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, !fresh, s);
         if (rc && rc != MRG_ENOCONV && !(bicg && rc == MRG_ENUMERIC)) return rc;
       } else if (!mixed) {
         MRG_CUDA(cudaMemsetAsync(w->du, 0, p->ndof * sizeof(double), s));

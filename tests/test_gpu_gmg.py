@@ -172,3 +172,54 @@ def test_gmg_bicgstab_entry_point(cuda):
     ro, Jo = O.assemble(np.zeros(O.ndof))
     xo, _, _ = O.pcg(Jo, ro, tol=1e-13, maxiter=100000)
     np.testing.assert_allclose(x.cpu().numpy(), xo, rtol=0, atol=1e-9 * np.abs(xo).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fp32", [False, True])
+def test_gmg_with_face_terms_matches_oracle(cuda, fp32):
+    """Weak-Dirichlet and Neumann faces keep their nodes free: the face terms enter the Galerkin hierarchy."""
+    from mrhyde_gb300 import AssemblyManager, SolverManager
+
+    c = _with_kappa(dict(dim=3, order=1, n=(20, 16, 12), dirichlet_faces=1), 6)
+    G, O = gpu_problem(c), oracle_problem(c)
+    for face, kind, okind in ((1, "weak_dirichlet", 2), (3, "neumann", 1), (5, "weak_dirichlet", 2)):
+        xyz = O.side_points(face)
+        g = np.cos(2.0 * xyz[:, 0]) * np.sin(1.5 * xyz[:, 1]) + 0.2 * face
+        O.set_face_bc(face, okind, g)
+        G.set_face_bc(face, kind, g)
+    A, S = AssemblyManager(G), SolverManager(G, preconditioner="gmg")
+    r, J = G.new_vector(), G.new_matrix_values(fp32=fp32)
+    A.assembleJacRes(G.new_vector(), r, J, fp32_jacobian=fp32, overwrite=True)
+    x = G.new_vector()
+    tol = 1e-5 if fp32 else 1e-11
+    res = S.PCG(J, r, x, tol=tol, maxiter=200)
+    assert res.rel_residual <= tol and res.iterations <= (12 if fp32 else 25), res.iterations
+    ro, Jo = O.assemble(np.zeros(O.ndof))
+    xo, _, _ = O.pcg(Jo, ro, tol=1e-13, maxiter=100000)
+    np.testing.assert_allclose(x.cpu().numpy(), xo, rtol=0, atol=(3e-4 if fp32 else 1e-9) * np.abs(xo).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order,fp32", [(1, False), (2, True)])
+def test_assembly_is_graph_capturable(cuda, order, fp32):
+    """mrg_assemble enqueues no host synchronisation: after a first call (which may allocate workspace),
+    the call can be captured in a CUDA graph and replaying it reproduces the direct result bit for bit."""
+    from mrhyde_gb300 import AssemblyManager
+
+    cfg = dict(dim=3, order=order, n=(6, 5, 4), kind="thermal" if order == 1 else "diffusion_1pu2",
+               dirichlet_faces=1, source=("const", 1.0, 0.0))
+    G = gpu_problem(cfg)
+    A = AssemblyManager(G)
+    u = torch.rand(G.info.n_dofs, dtype=torch.float64, device="cuda") * 0.3
+    r1, J1 = G.new_vector(), G.new_matrix_values(fp32=fp32)
+    A.assembleJacRes(u, r1, J1, fp32_jacobian=fp32, overwrite=True)
+    torch.cuda.synchronize()
+    r2, J2 = G.new_vector(), G.new_matrix_values(fp32=fp32)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            A.assembleJacRes(u, r2, J2, fp32_jacobian=fp32, overwrite=True, stream=s)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(r1, r2) and torch.equal(J1, J2)
