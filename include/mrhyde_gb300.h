@@ -32,7 +32,10 @@
  *   - J values must be laid out on the graph returned by mrg_get_graph (canonical structured numbering,
  *     sorted columns).
  *   - All work is enqueued on the caller's stream; nothing synchronises the host except the calls that
- *     return host-visible results (mrg_solve_pcg / mrg_newton statistics).
+ *     return host-visible results (mrg_solve_pcg / mrg_newton statistics).  mrg_assemble can be captured
+ *     in a CUDA graph once a first call has created its workspace (the Q2 FP32 Jacobian allocates its
+ *     tensor-core workspace on first use); a time-out inside the tensor-core kernel is reported by a
+ *     later Q2 FP32 Jacobian call instead of synchronising.
  *   - Every call returns an mrg_status; no C++ exception crosses the ABI.  mrg_last_error() gives text.
  *   - A handle is thread-compatible (one host thread at a time per handle).
  */
