@@ -125,11 +125,13 @@ __device__ __forceinline__ void sum_parts(const double* parts, double (&out)[K],
   if (threadIdx.x == 0) *counter = 0u;
 }
 
+// CSR row start of row n (nnz for n = nrows); PC > 0: compile-time polynomial order
+template <int PC = 0>
 __device__ __forceinline__ int64_t row_ptr_at(const Grid& g, int64_t n, int64_t nrows) {
   if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
   int ix, iy, iz;
   decompose(g, n, ix, iy, iz);
-  return row_info(g, ix, iy, iz).rp;
+  return row_info<PC>(g, ix, iy, iz).rp;
 }
 
 // ---- row products: y_i = sum_j J_ij x_j over the row of node i --------------------------------
@@ -258,7 +260,7 @@ __device__ __forceinline__ uintptr_t wtile_issue(const Grid& g, int64_t nrows, c
   const int64_t n0 = tile * WROWS;
   const int64_t n1 = (n0 + WROWS < nrows) ? n0 + WROWS : nrows;
   const int64_t nnz = g.T[0] * g.T[1] * g.T[2];
-  const int64_t seg0 = row_ptr_at(g, n0, nrows), seg1 = row_ptr_at(g, n1, nrows);
+  const int64_t seg0 = row_ptr_at<1>(g, n0, nrows), seg1 = row_ptr_at<1>(g, n1, nrows);
   const uintptr_t lo = (uintptr_t)(J + seg0), hi = (uintptr_t)(J + seg1);
   const uintptr_t base = lo & ~(uintptr_t)15;
   const uintptr_t jb = ((uintptr_t)J + 15) & ~(uintptr_t)15, je = (uintptr_t)(J + nnz) & ~(uintptr_t)15;
