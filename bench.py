@@ -219,11 +219,7 @@ def run_ours(args, rank, world, local_rank):
             ev[k][1].record(stream)
         barrier()
         ms = [a.elapsed_time(b) for a, b in ev]
-        tot = sum(ms)
-        if dist:
-            t = torch.tensor([tot], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
+        tot = max_over_ranks(sum(ms), dist, "cuda")
         return tot, ms
 
     jac64 = lambda: A.assembleJacRes(u, r, J64, overwrite=True)
@@ -352,7 +348,8 @@ def run_ours(args, rank, world, local_rank):
         out["solve"] = sol
 
     if not args.no_extras:
-        for name, fn in (("c3", bench_c3), ("c4", bench_c4), ("c5", bench_c5)):
+        for name, fn in (("c3", bench_c3), ("c4", bench_c4),
+                         ("c5", lambda a: bench_c5(a, rank, world, dist))):
             try:
                 out[name] = fn(args)
             except Exception as e:  # reported, never fatal for the headline line
@@ -461,24 +458,52 @@ def bench_c4(args):
             "mean_inner": float(st[:, 1].mean()), "all_converged": bool((st[:, 3] == 0).all())}
 
 
-def bench_c5(args):
+def max_over_ranks(x: float, dist=None, device="cpu") -> float:
+    """The largest value of x over all ranks (x itself on one process)."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def serve_replicated(reqs, slots, realtime, rank=0, world=1, dist=None):
+    """Serves this replica's share of `reqs`; on N replicas returns the whole-job summary (every rank)."""
+    from mrhyde_gb300 import serving
+
+    srv = serving.Server(hbm_budget_bytes=80 * 10**9, slots=slots)
+    mine = serving.shard(reqs, rank, world) if world > 1 else reqs
+    summ = srv.run(mine, realtime=realtime)
+    summ["peak_active"] = srv.peak_active
+    if world == 1 or dist is None:
+        return summ
+    parts = [None] * world
+    dist.all_gather_object(parts, ([r for r in srv.results], srv.wall))
+    whole = serving.merge(parts)
+    whole["peak_active"] = summ["peak_active"]
+    whole["replicas"] = world
+    return whole
+
+
+def bench_c5(args, rank=0, world=1, dist=None):
     """C5: Poisson stream (200 req/s) of thermal and nonlinear-diffusion solves on Q1 cubes with edge
     log-uniform in [16, 96], admitted under an 80 GB budget; p50/p99 latency and DOF/s, mixed vs FP64;
-    plus the batch throughput (all requests at t=0) and a stream at 80 % of it."""
+    plus the batch throughput (all requests at t=0) and a stream at 80 % of it.  On N GPUs the stream is
+    spread round-robin over N independent replicas and the figures are whole-job."""
     from mrhyde_gb300 import serving
 
     out = {}
     for mode in ("mixed", "fp64"):
         reqs = serving.poisson_stream(rate=200.0, count=args.c5_count, mixed=(mode == "mixed"), seed=5)
-        srv = serving.Server(hbm_budget_bytes=80 * 10**9, slots=args.c5_slots)
-        out[mode] = srv.run(reqs, realtime=True)
-        out[mode]["peak_active"] = srv.peak_active
+        out[mode] = serve_replicated(reqs, args.c5_slots, True, rank, world, dist)
     reqs = serving.poisson_stream(rate=200.0, count=args.c5_count, mixed=True, seed=5)
-    batch = serving.Server(hbm_budget_bytes=80 * 10**9, slots=args.c5_slots).run(reqs, realtime=False)
+    batch = serve_replicated(reqs, args.c5_slots, False, rank, world, dist)
     out["batch_mixed"] = batch
     rate80 = 0.8 * batch["req_per_s"]
     reqs = serving.poisson_stream(rate=rate80, count=args.c5_count, mixed=True, seed=6)
-    s80 = serving.Server(hbm_budget_bytes=80 * 10**9, slots=args.c5_slots).run(reqs, realtime=True)
+    s80 = serve_replicated(reqs, args.c5_slots, True, rank, world, dist)
     s80["rate"] = rate80
     s80["p99_over_p50"] = s80["p99_ms"] / s80["p50_ms"]
     out["stream_at_80pct_batch"] = s80

@@ -214,8 +214,22 @@ class Server:
             self._lock.notify_all()
         for w in workers:
             w.join()
-        wall = time.perf_counter() - t0
-        return summarize(self.results, wall)
+        self.wall = time.perf_counter() - t0
+        return summarize(self.results, self.wall)
+
+
+def shard(requests, rank: int, world: int):
+    """The requests replica `rank` of `world` serves: round-robin by request id (a front end spreading one
+    Poisson stream over independent replicas; each replica sees a thinned Poisson stream)."""
+    return [r for r in requests if r.rid % world == rank]
+
+
+def merge(parts):
+    """Whole-job summary from the replicas' (results, wall) pairs: latencies pooled, throughput over the
+    longest replica wall time."""
+    results = [r for res, _ in parts for r in res]
+    wall = max((w for _, w in parts), default=0.0)
+    return summarize(results, wall)
 
 
 def summarize(results, wall):
