@@ -523,6 +523,18 @@ def run_profile(args, local_rank):
 
     torch.cuda.set_device(local_rank)
     mrhyde_gb300.load()
+    if args.profile == "c4":  # the batched subgrid solve, default configuration (no autotuning)
+        from mrhyde_gb300.subgrid import SubgridBatch
+        from mrhyde_gb300.workloads import c4_problem, c4_sizes
+
+        sizes = c4_sizes(4096, seed=4)
+        probs = [c4_problem(sizes, k, seed=4) for k in range(len(sizes))]
+        B = SubgridBatch(sizes, [p["kappa"] for p in probs], [p["dirichlet"][1] for p in probs], source=1.0)
+        for _ in range(args.warmup + args.steps):
+            B.solve(stats=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "c4", "steps": args.steps, "ok": True}))
+        return
     if args.profile in ("q2tc", "q2cc"):
         from mrhyde_gb300.workloads import c3
 
@@ -576,7 +588,7 @@ def main():
     ap.add_argument("--c3-n", type=int, default=64)
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32"],
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c4"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
