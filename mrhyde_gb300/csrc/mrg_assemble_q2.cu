@@ -156,16 +156,19 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
     Fz = cw * T.s[2] * T.s[2] * gz;
     if (mode & 2) {
       QT* qb = qbuf + cid * K::NQB;
-      // tc_image (FP32 only): split x = hi + lo (hi = x rounded to TF32, lo = the remainder rounded to
+      // tc_image (FP32 only): split x = hi + lo (hi = x rounded to TF32, lo = the FP32 remainder rounded to
       // TF32) and store both into the tensor-core operand image [tile][hi, lo][K chunk][cell][4] with
       // 128-cell tiles and 112 K slots; otherwise plain QT values [cell][4 NL]
       auto put = [&](int k, double v) {
         if constexpr (sizeof(QT) == 4) {
           if (tc_image) {
-            const float hi = tf32_rn((float)v);
+            // split of the FP32 value (the remainder is exact in FP32; 3xTF32 keeps ~22 bits anyway):
+            // one FP64 -> FP32 conversion per value, the rest on the FP32 pipe
+            const float f = (float)v;
+            const float hi = tf32_rn(f);
             float* t = qbuf + (cid >> 7) * (2 * 128 * 112) + (k >> 2) * 512 + (cid & 127) * 4 + (k & 3);
             t[0] = hi;
-            t[128 * 112] = tf32_rn((float)(v - (double)hi));
+            t[128 * 112] = tf32_rn(f - hi);
             return;
           }
         }

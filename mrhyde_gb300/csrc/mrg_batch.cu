@@ -74,17 +74,24 @@ struct BatchArgs {
   int max_outer, max_inner;
 };
 
+// Block sum of FP32 per-thread partials: FP32 warp tree, one conversion per warp, the warp partials
+// added in FP64 by one thread in a fixed order, the result broadcast.  Costs the FP64 pipe T/32 + 1
+// operations per block instead of ~15 per thread (it runs several times per inner iteration).
 template <int T>
-__device__ __forceinline__ double bsum(double v, double* sh) {
+__device__ __forceinline__ double bsumf(float v, double* sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)v;
   __syncthreads();
-  double s = 0.0;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
 #pragma unroll
-  for (int i = 0; i < T / 32; ++i) s += sh[i];
-  return s;  // same value in every thread, fixed order
+    for (int i = 0; i < T / 32; ++i) s += sh[i];
+    sh[T / 32] = s;
+  }
+  __syncthreads();
+  return sh[T / 32];  // same value in every thread, fixed order
 }
 
 template <int T>
@@ -114,7 +121,7 @@ template <int T, int R>
 __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* p_sh = reinterpret_cast<float*>(smem_raw);
-  __shared__ double red[T / 32];
+  __shared__ double red[T / 32 + 1];
   __shared__ int s_idx;
   for (;;) {
     __syncthreads();
@@ -135,11 +142,13 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
     // ---- 1. Dirichlet data; 2. FP32 Jacobian (+ Jacobi diagonal); p = 0 ----
     float minv[R];
     bool interior[R];
+    int rp32[R];  // CSR offset of each interior row within the problem (set once, used every iteration)
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const int i = threadIdx.x + k * T;
       interior[k] = false;
       minv[k] = 0.0f;
+      rp32[k] = 0;
       if (i >= nn) continue;
       const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
       const bool inside = ix > 0 && ix < NX - 1 && iy > 0 && iy < NY - 1 && iz > 0 && iz < NZ - 1;
@@ -192,6 +201,7 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
       const float dg = -(osum + ocomp);
       J[rp + 13] = dg;
       minv[k] = 1.0f / dg;
+      rp32[k] = (int)rp;
     }
     __syncthreads();
     // ---- 3./4. refinement loop ----
@@ -251,8 +261,11 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
       if (!isfinite(rnorm)) { status = MRG_ENUMERIC; break; }
       if (rnorm == 0.0 || rnorm <= A.tol * r0 || outer >= A.max_outer) break;
       // FP32 Jacobi PCG on J32 d = r (x0 = 0)
+      // Dot products: each thread sums its (at most R) rows in FP32 and converts once; the block sum is
+      // FP64.  (Per-row FP64 accumulation costs a conversion and an add on the FP64 pipe per row and
+      // iteration, which on GB300 runs at 1/64 of the FP32 rate.)
       float x[R], r[R], z[R];
-      double rr = 0.0, rz = 0.0;
+      float rrf = 0.0f, rzf = 0.0f;
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const int i = threadIdx.x + k * T;
@@ -260,25 +273,23 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
         r[k] = (float)r64[k];
         z[k] = r[k] * minv[k];
         if (i < nn) p_sh[i] = z[k];
-        rr += (double)(r[k] * r[k]);
-        rz += (double)(r[k] * z[k]);
+        rrf = fmaf(r[k], r[k], rrf);
+        rzf = fmaf(r[k], z[k], rzf);
       }
-      rr = bsum<T>(rr, red);
-      double rho = bsum<T>(rz, red);
-      const double rr0 = sqrt(rr);
+      double rr = bsumf<T>(rrf, red);
+      double rho = bsumf<T>(rzf, red);
+      const double stop2 = A.inner_tol * A.inner_tol * rr;  // ||r||^2 threshold of the inner solve
       int it = 0;
-      while (it < A.max_inner && sqrt(rr) > A.inner_tol * rr0 && rr0 > 0.0) {
+      while (it < A.max_inner && rr > stop2 && stop2 > 0.0) {
         // q = J p  (stored FP32 Jacobian rows, p from shared memory)
         float q[R];
-        double pq = 0.0;
+        float pqf = 0.0f;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
           q[k] = 0.0f;
           const int i = threadIdx.x + k * T;
           if (i >= nn || !interior[k]) continue;
-          const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
-          const int64_t rp = axis_prefix(iz, NZ) * Ty * Tx + 3LL * (axis_prefix(iy, NY) * Tx + 3LL * axis_prefix(ix, NX));
-          const float* row = J + rp;
+          const float* row = J + rp32[k];
           float acc = 0.0f;
 #pragma unroll
           for (int dz = -1; dz <= 1; ++dz)
@@ -288,13 +299,13 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
               for (int dx = -1; dx <= 1; ++dx)
                 acc = fmaf(row[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)], p_sh[i + dx + NX * (dy + NY * dz)], acc);
           q[k] = acc;
-          pq += (double)(acc * p_sh[i]);
+          pqf = fmaf(acc, p_sh[i], pqf);
         }
-        pq = bsum<T>(pq, red);
+        const double pq = bsumf<T>(pqf, red);
         if (!(pq > 0.0)) { status = MRG_ENUMERIC; break; }
-        const float alpha = (float)(rho / pq);
-        rr = 0.0;
-        rz = 0.0;
+        const float alpha = (float)rho / (float)pq;  // FP32 division (the inner solve is FP32)
+        rrf = 0.0f;
+        rzf = 0.0f;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
           const int i = threadIdx.x + k * T;
@@ -302,12 +313,12 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
           x[k] = fmaf(alpha, p_sh[i], x[k]);
           r[k] = fmaf(-alpha, q[k], r[k]);
           z[k] = r[k] * minv[k];
-          rr += (double)(r[k] * r[k]);
-          rz += (double)(r[k] * z[k]);
+          rrf = fmaf(r[k], r[k], rrf);
+          rzf = fmaf(r[k], z[k], rzf);
         }
-        rr = bsum<T>(rr, red);
-        rz = bsum<T>(rz, red);
-        const float beta = (float)(rz / rho);
+        rr = bsumf<T>(rrf, red);
+        const double rz = bsumf<T>(rzf, red);
+        const float beta = (float)rz / (float)rho;
         rho = rz;
 #pragma unroll
         for (int k = 0; k < R; ++k) {

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(BT) k_b_spmv(Grid g, int64_t nrows, BVec<VT, J
   if (BDONE(V)) return;
   const VT* in = (STEP == 0) ? V.ph : V.sh;
   VT* out = (STEP == 0) ? V.v : V.t;
-  double d0 = 0.0, d1 = 0.0;
+  VT d0 = VT(0), d1 = VT(0);  // per-thread partials in the vector precision, block sums in FP64
   GSTRIDE(n) {
     int ix, iy, iz;
     decompose(g, n, ix, iy, iz);
@@ -106,13 +106,13 @@ __global__ void __launch_bounds__(BT) k_b_spmv(Grid g, int64_t nrows, BVec<VT, J
     const VT y = row_dot<P, JT, VT, VT>(g, R, V.J + R.rp, in);
     out[n] = y;
     if (STEP == 0) {
-      d0 += (double)(V.rh[n] * y);
+      d0 = fma(V.rh[n], y, d0);
     } else {
-      d0 += (double)(y * V.s[n]);
-      d1 += (double)(y * y);
+      d0 = fma(y, V.s[n], d0);
+      d1 = fma(y, y, d1);
     }
   }
-  double m[2] = {block_sum(d0), block_sum(d1)};
+  double m[2] = {block_sum((double)d0), block_sum((double)d1)};
   if (last_block<2>(V.parts, m, &V.S->counter)) {
     double t[2];
     sum_parts<2>(V.parts, t, &V.S->counter);
@@ -148,15 +148,15 @@ template <typename VT, typename JT>
 __global__ void __launch_bounds__(BT) k_b_update(int64_t nrows, BVec<VT, JT> V) {
   if (BDONE(V)) return;
   const VT alpha = (VT)V.S->alpha, omega = (VT)V.S->omega;
-  double rr = 0.0, rhr = 0.0;
+  VT rr = VT(0), rhr = VT(0);
   GSTRIDE(n) {
     V.x[n] += alpha * V.ph[n] + omega * V.sh[n];
     const VT r = V.s[n] - omega * V.t[n];
     V.r[n] = r;
-    rr += (double)(r * r);
-    rhr += (double)(V.rh[n] * r);
+    rr = fma(r, r, rr);
+    rhr = fma(V.rh[n], r, rhr);
   }
-  double m[2] = {block_sum(rr), block_sum(rhr)};
+  double m[2] = {block_sum((double)rr), block_sum((double)rhr)};
   if (last_block<2>(V.parts, m, &V.S->counter)) {
     double t[2];
     sum_parts<2>(V.parts, t, &V.S->counter);

@@ -204,10 +204,10 @@ __global__ void __launch_bounds__(NT) k_diag(Grid g, const T* __restrict__ A, T*
     const T* vals = A + R.rp;
     const int len = R.cx * R.cy * R.cz;
     const T dgv = vals[diag_pos(R, ix, iy, iz) - R.rp];
-    double s = 0.0;
-    for (int e = 0; e < len; ++e) s += fabs((double)vals[e]);
+    T s = T(0);  // a bound: the level's precision is enough
+    for (int e = 0; e < len; ++e) s += fabs(vals[e]);
     minv[n] = T(1) / dgv;
-    v = (float)(s / fabs((double)dgv));
+    v = (float)(s / fabs(dgv));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
@@ -271,22 +271,35 @@ __global__ void __launch_bounds__(NT) k_coarse_inv(Grid g, const T* __restrict__
 // ---- cycle kernels --------------------------------------------------------------------------------
 // Chebyshev step `k` (0..NU-1): d = rho_k rho_{k-1} d + (2 rho_k / delta) D^{-1}(b - A x)  (k = 0:
 // d = D^{-1}(b - A x) / theta); xout = x + d.  zero_x: x = 0 (no SpMV).
+// Chebyshev coefficients of every level and step (one thread per level, at setup): coef[(l NU + k) 3 + m]
+// = {1/theta, rho_k rho_{k-1}, 2 rho_k / delta} on [CHEB_LO L, L], L the level's Gershgorin bound.
+__global__ void k_cheb_coef(const unsigned int* __restrict__ lmax_bits, int nlev, double* __restrict__ coef) {
+  const int l = threadIdx.x;
+  if (l >= nlev) return;
+  const double hi = (double)__uint_as_float(lmax_bits[l]), lo = CHEB_LO * hi;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  double rho_prev = 1.0 / sigma, rho = rho_prev;
+  for (int k = 0; k < NU; ++k) {
+    if (k > 0) {
+      const double rn = 1.0 / (2.0 * sigma - rho);
+      rho_prev = rho;
+      rho = rn;
+    }
+    double* c = coef + ((size_t)l * NU + k) * 3;
+    c[0] = 1.0 / theta;
+    c[1] = rho * rho_prev;
+    c[2] = 2.0 * rho / delta;
+  }
+}
+
 template <int P, typename T>
 __global__ void __launch_bounds__(NT) k_cheb(LevDev<T> L, const T* __restrict__ xin, T* __restrict__ xout, int k,
-                                             int zero_x, const unsigned int* __restrict__ lmax_bits,
+                                             int zero_x, const double* __restrict__ coef,
                                              const GScal* __restrict__ S, int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
   if (is_done(S)) return;
-  const double hi = (double)__uint_as_float(*lmax_bits), lo = CHEB_LO * hi;
-  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
-  double rho_prev = 1.0 / sigma, rho = rho_prev;
-  for (int j = 1; j <= k; ++j) {
-    const double rn = 1.0 / (2.0 * sigma - rho);
-    rho_prev = rho;
-    rho = rn;
-  }
-  const T c_old = (T)(rho * rho_prev), c_new = (T)(2.0 * rho / delta), c_first = (T)(1.0 / theta);
+  const T c_first = (T)coef[3 * k], c_old = (T)coef[3 * k + 1], c_new = (T)coef[3 * k + 2];
   auto fin = [&](int64_t n, T ax) {
     const T z = L.minv[n] * (L.b[n] - ax);
     const T d = (k == 0) ? c_first * z : c_old * L.d[n] + c_new * z;
@@ -398,16 +411,16 @@ struct CgVec {
 // x = 0, r = b (FP64 in, T out), p = q = 0; r0 = |r|
 template <typename T>
 __global__ void __launch_bounds__(NT) k_cg_init(int64_t n, const double* __restrict__ b, CgVec<T> V) {
-  double rr = 0.0;
+  T rr = T(0);  // per-thread partials in the vector precision (no per-element FP64 work for FP32)
   for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
     const T r = (T)b[i];
     V.x[i] = T(0);
     V.r[i] = r;
     V.p[i] = T(0);
     V.q[i] = T(0);
-    rr += (double)r * (double)r;
+    rr = fma(r, r, rr);
   }
-  double m[1] = {block_sum(rr)};
+  double m[1] = {block_sum((double)rr)};
   if (last_block<1>(V.parts, m, &V.S->counter)) {
     double t[1];
     sum_parts<1>(V.parts, t, &V.S->counter);
@@ -429,10 +442,10 @@ __global__ void __launch_bounds__(NT) k_cg_init(int64_t n, const double* __restr
 template <typename T>
 __global__ void __launch_bounds__(NT) k_cg_rz(int64_t n, CgVec<T> V, int first) {
   if (is_done(V.S)) return;
-  double rz = 0.0;
+  T rz = T(0);
   for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
-    rz += (double)V.r[i] * (double)V.z[i];
-  double m[1] = {block_sum(rz)};
+    rz = fma(V.r[i], V.z[i], rz);
+  double m[1] = {block_sum((double)rz)};
   if (last_block<1>(V.parts, m, &V.S->counter)) {
     double t[1];
     sum_parts<1>(V.parts, t, &V.S->counter);
@@ -452,17 +465,17 @@ __global__ void __launch_bounds__(NT) k_cg_spmv(Grid g, int64_t n, const T* __re
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
   if (is_done(V.S)) return;
   const T beta = (T)V.S->beta;
-  double pq = 0.0;
+  T pq = T(0);
   const bool ok = level_rows<P, T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
     const T w = (T)row_prod<P, T>(g, R, vals, V.z);
     const T pn = V.z[i] + beta * V.p[i];
     const T qn = w + beta * V.q[i];
     V.p[i] = pn;
     V.q[i] = qn;
-    pq += (double)pn * (double)qn;
+    pq = fma(pn, qn, pq);
   });
   if (!ok) atomicExch(&V.S->err, 3);
-  double m[1] = {block_sum(pq)};
+  double m[1] = {block_sum((double)pq)};
   if (last_block<1>(V.parts, m, &V.S->counter)) {
     double t[1];
     sum_parts<1>(V.parts, t, &V.S->counter);
@@ -481,14 +494,14 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_cg_update(int64_t n, CgVec<T> V) {
   if (is_done(V.S)) return;
   const T alpha = (T)V.S->alpha;
-  double rr = 0.0;
+  T rr = T(0);
   for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
     V.x[i] += alpha * V.p[i];
     const T r = V.r[i] - alpha * V.q[i];
     V.r[i] = r;
-    rr += (double)r * (double)r;
+    rr = fma(r, r, rr);
   }
-  double m[1] = {block_sum(rr)};
+  double m[1] = {block_sum((double)rr)};
   if (last_block<1>(V.parts, m, &V.S->counter)) {
     double t[1];
     sum_parts<1>(V.parts, t, &V.S->counter);
@@ -519,7 +532,7 @@ struct BgVec {
 // x = 0, r = rh = b, p = v = 0; rho = (rh . r), alpha = omega = 1, beta = 0
 template <typename T>
 __global__ void __launch_bounds__(NT) k_bg_init(int64_t n, const double* __restrict__ b, BgVec<T> V) {
-  double rr = 0.0;
+  T rr = T(0);
   for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
     const T r = (T)b[i];
     V.x[i] = T(0);
@@ -527,9 +540,9 @@ __global__ void __launch_bounds__(NT) k_bg_init(int64_t n, const double* __restr
     V.rh[i] = r;
     V.p[i] = T(0);
     V.v[i] = T(0);
-    rr += (double)r * (double)r;
+    rr = fma(r, r, rr);
   }
-  double m[1] = {block_sum(rr)};
+  double m[1] = {block_sum((double)rr)};
   if (last_block<1>(V.parts, m, &V.S->counter)) {
     double t[1];
     sum_parts<1>(V.parts, t, &V.S->counter);
@@ -566,19 +579,19 @@ __global__ void __launch_bounds__(NT) k_bg_spmv(Grid g, int64_t n, const T* __re
   if (is_done(V.S)) return;
   const T* in = STEP == 0 ? V.ph : V.sh;
   T* out = STEP == 0 ? V.v : V.t;
-  double d0 = 0.0, d1 = 0.0;
+  T d0 = T(0), d1 = T(0);
   const bool ok = level_rows<P, T>(g, n, A, smem_raw, mbar, [&](int64_t i, const RowInfo& R, const T* vals) {
     const T y = (T)row_prod<P, T>(g, R, vals, in);
     out[i] = y;
     if (STEP == 0) {
-      d0 += (double)V.rh[i] * (double)y;
+      d0 = fma(V.rh[i], y, d0);
     } else {
-      d0 += (double)y * (double)V.s[i];
-      d1 += (double)y * (double)y;
+      d0 = fma(y, V.s[i], d0);
+      d1 = fma(y, y, d1);
     }
   });
   if (!ok) atomicExch(&V.S->err, 3);
-  double m[2] = {block_sum(d0), block_sum(d1)};
+  double m[2] = {block_sum((double)d0), block_sum((double)d1)};
   if (last_block<2>(V.parts, m, &V.S->counter)) {
     double t[2];
     sum_parts<2>(V.parts, t, &V.S->counter);
@@ -610,15 +623,15 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_bg_update(int64_t n, BgVec<T> V) {
   if (is_done(V.S)) return;
   const T alpha = (T)V.S->alpha, omega = (T)V.S->omega;
-  double rr = 0.0, rhr = 0.0;
+  T rr = T(0), rhr = T(0);
   for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
     V.x[i] += alpha * V.ph[i] + omega * V.sh[i];
     const T r = V.s[i] - omega * V.t[i];
     V.r[i] = r;
-    rr += (double)r * (double)r;
-    rhr += (double)V.rh[i] * (double)r;
+    rr = fma(r, r, rr);
+    rhr = fma(V.rh[i], r, rhr);
   }
-  double m[2] = {block_sum(rr), block_sum(rhr)};
+  double m[2] = {block_sum((double)rr), block_sum((double)rhr)};
   if (last_block<2>(V.parts, m, &V.S->counter)) {
     double t[2];
     sum_parts<2>(V.parts, t, &V.S->counter);
@@ -677,6 +690,7 @@ struct Hier {
   T* cinv = nullptr;
   T* mid[2] = {nullptr, nullptr};  // intermediate operators of the Galerkin sweeps
   unsigned int* lmax = nullptr;   // [nlev] float bits
+  double* coef = nullptr;         // [nlev][NU][3] Chebyshev coefficients
   int* err = nullptr;             // setup / cycle error word
   T *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr;  // CG vectors (level-0 size)
   double* parts = nullptr;
@@ -752,7 +766,7 @@ void free_hier(Hier<T>* H, cudaStream_t s) {
   }
   for (void* ptr : {(void*)H->mid[0], (void*)H->mid[1]})
     if (ptr) cudaFreeAsync(ptr, s);
-  for (void* ptr : {(void*)H->cinv, (void*)H->lmax, (void*)H->err, (void*)H->x, (void*)H->r, (void*)H->p,
+  for (void* ptr : {(void*)H->cinv, (void*)H->lmax, (void*)H->coef, (void*)H->err, (void*)H->x, (void*)H->r, (void*)H->p,
                     (void*)H->q, (void*)H->parts, (void*)H->S})
     if (ptr) cudaFreeAsync(ptr, s);
   if (H->h_S) cudaFreeHost(H->h_S);
@@ -841,6 +855,7 @@ int build_hier(const mrg_problem* p, Hier<T>*& out, cudaStream_t s) {
   const size_t nparts = (size_t)2 * grid_for(n0, 16) + 64;
   if (cudaMallocAsync(&H->cinv, (size_t)nc * nc * sizeof(T), s) != cudaSuccess ||
       cudaMallocAsync(&H->lmax, MAXLEV * sizeof(unsigned int), s) != cudaSuccess ||
+      cudaMallocAsync(&H->coef, (size_t)MAXLEV * NU * 3 * sizeof(double), s) != cudaSuccess ||
       cudaMallocAsync(&H->err, sizeof(int), s) != cudaSuccess ||
       cudaMallocAsync(&H->x, n0 * sizeof(T), s) != cudaSuccess || cudaMallocAsync(&H->r, n0 * sizeof(T), s) != cudaSuccess ||
       cudaMallocAsync(&H->p, n0 * sizeof(T), s) != cudaSuccess || cudaMallocAsync(&H->q, n0 * sizeof(T), s) != cudaSuccess ||
@@ -909,6 +924,7 @@ int setup_values(Hier<T>* H, const T* J, cudaStream_t s) {
     MRG_CUDA(cudaGetLastError());
   }
   k_coarse_inv<T><<<1, NT, 0, s>>>(H->L.back().g, (const T*)H->L.back().A, H->cinv, H->err);
+  k_cheb_coef<<<1, 32, 0, s>>>(H->lmax, nl, H->coef);
   MRG_CUDA(cudaGetLastError());
   return MRG_OK;
 }
@@ -917,13 +933,13 @@ int setup_values(Hier<T>* H, const T* J, cudaStream_t s) {
 // CTAs per SM), a Q2 level 0 the direct row loop.
 template <typename T>
 void launch_cheb(const HLevel& L, const LevDev<T>& D, const T* xin, T* xout, int k, int zero_x,
-                 const unsigned int* lmax, const GScal* S, int* err, cudaStream_t s) {
+                 const double* coef, const GScal* S, int* err, cudaStream_t s) {
   if (zero_x)
-    k_cheb<1, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, xin, xout, k, 1, lmax, S, err);
+    k_cheb<1, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, xin, xout, k, 1, coef, S, err);
   else if (L.pp.p[0] == 2)
-    k_cheb<2, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, xin, xout, k, 0, lmax, S, err);
+    k_cheb<2, T><<<grid_for(D.n, 16), NT, 0, s>>>(D, xin, xout, k, 0, coef, S, err);
   else
-    k_cheb<1, T><<<grid_for(D.n, staged_per_sm<T>()), NT, staged_smem<T>(), s>>>(D, xin, xout, k, 0, lmax, S, err);
+    k_cheb<1, T><<<grid_for(D.n, staged_per_sm<T>()), NT, staged_smem<T>(), s>>>(D, xin, xout, k, 0, coef, S, err);
 }
 
 template <typename T>
@@ -941,8 +957,8 @@ void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
     LevDev<T> D = levdev<T>(H->L[l]);
     if (l == 0) D.b = const_cast<T*>(in);
     // pre-smoothing from x = 0: xa <- step 0, xb <- step 1
-    launch_cheb<T>(H->L[l], D, D.xa, D.xa, 0, 1, H->lmax + l, S, H->err, s);
-    launch_cheb<T>(H->L[l], D, D.xa, D.xb, 1, 0, H->lmax + l, S, H->err, s);
+    launch_cheb<T>(H->L[l], D, D.xa, D.xa, 0, 1, H->coef + (size_t)l * NU * 3, S, H->err, s);
+    launch_cheb<T>(H->L[l], D, D.xa, D.xb, 1, 0, H->coef + (size_t)l * NU * 3, S, H->err, s);
     launch_resid<T>(H->L[l], D, D.xb, S, H->err, s);
     const HLevel& C = H->L[l + 1];
     k_restrict<T><<<grid_for(C.n, 16), NT, 0, s>>>(D.g, C.g, C.X, D.r, (T*)C.b, S);
@@ -955,8 +971,8 @@ void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
     const HLevel& C = H->L[l + 1];
     k_prolong<T><<<grid_for(D.n, 16), NT, 0, s>>>(D.g, C.g, C.X, (const T*)C.xb, D.xb, S);
     // post-smoothing: xb -> xa (step 0), xa -> xb (step 1; level 0: -> out)
-    launch_cheb<T>(H->L[l], D, D.xb, D.xa, 0, 0, H->lmax + l, S, H->err, s);
-    launch_cheb<T>(H->L[l], D, D.xa, l == 0 ? out : D.xb, 1, 0, H->lmax + l, S, H->err, s);
+    launch_cheb<T>(H->L[l], D, D.xb, D.xa, 0, 0, H->coef + (size_t)l * NU * 3, S, H->err, s);
+    launch_cheb<T>(H->L[l], D, D.xa, l == 0 ? out : D.xb, 1, 0, H->coef + (size_t)l * NU * 3, S, H->err, s);
   }
 }
 
