@@ -23,6 +23,7 @@
 //      into r and res.dx into its CSR row (slots computed analytically).  Cells are processed in
 //      2^dim colours so that no two cells of one launch share a node (non-atomic RMW), or in one
 //      launch with atomics (MRG_ASM_ATOMIC).
+#include <cmath>
 #include <cstdio>
 
 #include "mrg_internal.h"
@@ -98,6 +99,7 @@ struct FactArgs {
   double Kp[8];
   float Kp32[8];
   double load;        // f * int(phi_l) over one cell (constant source)
+  double loadk[4];    // load * 2^k (k = axes on which the node is interior): b_i without FP64 instructions
   int src_sin;        // 1: b_i = amp * Bx[ix] * By[iy] (* Bz[iz])
   double amp;
   const double* B[3];
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double*
       // load vector entry b_i
       double b;
       if (A.src_sin) b = A.amp * A.B[0][ix] * A.B[1][iy] * A.B[2][iz];
-      else b = A.load * (double)((cx == 3 ? 2 : 1) * (cy == 3 ? 2 : 1) * (cz == 3 ? 2 : 1));
+      else b = A.loadk[(cx == 3) + (cy == 3) + (cz == 3)];
       double acc = b;
       double t[8];
 #pragma unroll
@@ -363,7 +365,7 @@ __global__ void __launch_bounds__(FT) k_fact_quad(const FactArgs A, const double
       }
       double b;
       if (A.src_sin) b = A.amp * A.B[0][ix] * A.B[1][iy];
-      else b = A.load * (double)((cx == 3 ? 2 : 1) * (cy == 3 ? 2 : 1));
+      else b = A.loadk[(cx == 3) + (cy == 3)];
       double acc = b, t[4] = {0.0, 0.0, 0.0, 0.0};
       float osum = 0.0f, ocomp = 0.0f;
       int dpos = 0;
@@ -758,6 +760,7 @@ int mrg_launch_factored(mrg_problem* p, const double* u, double* r, void* J, uin
   A.src_sin = (p->source_kind == MRG_SRC_SINPROD);
   A.amp = p->source_amp;
   A.load = p->source_amp * p->cell_load;
+  for (int k = 0; k < 4; ++k) A.loadk[k] = std::ldexp(A.load, k);  // exact: a power-of-two scaling
   if (A.src_sin) {
     A.B[0] = p->d_srcB;
     A.B[1] = p->d_srcB + p->g.nn[0];

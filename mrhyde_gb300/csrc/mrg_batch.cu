@@ -72,26 +72,37 @@ struct BatchArgs {
   mrg_batch_stat* stats;
   double tol, inner_tol;
   int max_outer, max_inner;
+  int max_nodes;  // nodes of the largest problem: length of each shared-memory array
 };
 
-// Block sum of FP32 per-thread partials: FP32 warp tree, one conversion per warp, the warp partials
-// added in FP64 by one thread in a fixed order, the result broadcast.  Costs the FP64 pipe T/32 + 1
-// operations per block instead of ~15 per thread (it runs several times per inner iteration).
+// Block sums of FP32 per-thread partials (the inner solve is FP32): warp tree, one partial per warp in
+// shared memory, one barrier, then every thread adds the warp partials in the same fixed order (same
+// value everywhere, independent of scheduling).  The partial buffers alternate between two halves, so a
+// reduction never overwrites partials that a slower thread may still be reading from the previous one:
+// between a write to a half and the previous reads of that half lies the barrier of the reduction in
+// between.
 template <int T>
-__device__ __forceinline__ double bsumf(float v, double* sh) {
+__device__ __forceinline__ float2 bsum2(float a, float b, float* red, int& half) {
+  constexpr int NW = T / 32;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-#pragma unroll
-    for (int i = 0; i < T / 32; ++i) s += sh[i];
-    sh[T / 32] = s;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  float* buf = red + half * (2 * NW);
+  if ((threadIdx.x & 31) == 0) {
+    buf[threadIdx.x >> 5] = a;
+    buf[NW + (threadIdx.x >> 5)] = b;
   }
   __syncthreads();
-  return sh[T / 32];  // same value in every thread, fixed order
+  float sa = 0.0f, sb = 0.0f;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    sa += buf[w];
+    sb += buf[NW + w];
+  }
+  half ^= 1;
+  return make_float2(sa, sb);
 }
 
 template <int T>
@@ -116,13 +127,20 @@ __device__ __forceinline__ void nstep_add(float& sum, float& comp, float v) {
   sum = t;
 }
 
-// R = max rows per thread
+// R = max rows per thread.  Registers hold only the residual r and the SpMV result q of the thread's
+// rows; the correction x, the Jacobi inverse, the CSR row offsets and the search direction p live in
+// shared memory (4 floats per node of the largest problem), which leaves room for several CTAs per SM.
 template <int T, int R>
 __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* p_sh = reinterpret_cast<float*>(smem_raw);
-  __shared__ double red[T / 32 + 1];
+  float* x_sh = p_sh + A.max_nodes;
+  float* mi_sh = x_sh + A.max_nodes;
+  int* rp_sh = reinterpret_cast<int*>(mi_sh + A.max_nodes);
+  __shared__ float red[2 * 2 * (T / 32)];
+  __shared__ double redd[T / 32];
   __shared__ int s_idx;
+  int half = 0;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_idx = atomicAdd(A.counter, 1);
@@ -139,24 +157,23 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
     float* J = A.J + P.nnz_off;
     const double* gv = A.g + P.node_off;
     const int64_t Tx = 3LL * NX - 2, Ty = 3LL * NY - 2;
-    // ---- 1. Dirichlet data; 2. FP32 Jacobian (+ Jacobi diagonal); p = 0 ----
-    float minv[R];
-    bool interior[R];
-    int rp32[R];  // CSR offset of each interior row within the problem (set once, used every iteration)
+    // rows of this thread: i = threadIdx.x + k T for k < kn
+    const int kn = nn > (int)threadIdx.x ? (nn - (int)threadIdx.x + T - 1) / T : 0;
+    // ---- 1. Dirichlet data; 2. FP32 Jacobian (+ Jacobi inverse); p = 0 ----
+    unsigned interior = 0u;  // bit k: row k of this thread is a free (interior) row
 #pragma unroll
     for (int k = 0; k < R; ++k) {
+      if (k >= kn) break;
       const int i = threadIdx.x + k * T;
-      interior[k] = false;
-      minv[k] = 0.0f;
-      rp32[k] = 0;
-      if (i >= nn) continue;
       const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
       const bool inside = ix > 0 && ix < NX - 1 && iy > 0 && iy < NY - 1 && iz > 0 && iz < NZ - 1;
-      interior[k] = inside;
+      interior |= (inside ? 1u : 0u) << k;
       u[i] = inside ? 0.0 : gv[i];
       p_sh[i] = 0.0f;
       const int cxn = axis_count(ix, NX), cyn = axis_count(iy, NY), czn = axis_count(iz, NZ);
       const int64_t rp = axis_prefix(iz, NZ) * Ty * Tx + (int64_t)czn * (axis_prefix(iy, NY) * Tx + (int64_t)cyn * axis_prefix(ix, NX));
+      rp_sh[i] = (int)rp;
+      mi_sh[i] = 0.0f;
       if (!inside) {
         // Dirichlet row: identity (never scattered, J(d,d) = 1)
         const int lx = ix > 0 ? ix - 1 : 0, ly = iy > 0 ? iy - 1 : 0, lz = iz > 0 ? iz - 1 : 0;
@@ -200,22 +217,24 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
           }
       const float dg = -(osum + ocomp);
       J[rp + 13] = dg;
-      minv[k] = 1.0f / dg;
-      rp32[k] = (int)rp;
+      mi_sh[i] = 1.0f / dg;
     }
     __syncthreads();
     // ---- 3./4. refinement loop ----
     double r0 = 0.0, rnorm = 0.0;
     int outer = 0, inner_tot = 0, status = MRG_OK;
     for (;;) {
-      // FP64 residual at u (matrix-free factored form)
-      double r64[R];
+      // FP64 residual at u (matrix-free factored form): per offset class c, t_c = sum S(off) u(i+off),
+      // then r = b - sum_c K_c t_c (35 FP64 FMAs a row instead of 54 multiplies and FMAs)
+      float r[R];
       double amax = 0.0;
 #pragma unroll
+      for (int k = 0; k < R; ++k) r[k] = 0.0f;
+#pragma unroll
       for (int k = 0; k < R; ++k) {
-        r64[k] = 0.0;
+        if (k >= kn) break;
+        if (!((interior >> k) & 1u)) continue;
         const int i = threadIdx.x + k * T;
-        if (i >= nn || !interior[k]) continue;
         const int ix = i % NX, iy = (i / NX) % NY, iz = i / (NX * NY);
         double kk[2][2][2];
 #pragma unroll
@@ -242,7 +261,9 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
             sxy[c][1][x] = sx[c][0][x] + sx[c][1][x];
             sxy[c][2][x] = sx[c][1][x];
           }
-        double acc = P.load * 8.0;
+        double t[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) t[c] = 0.0;
 #pragma unroll
         for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
@@ -251,45 +272,49 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
             for (int dx = 0; dx < 3; ++dx) {
               const double s = (dz == 0) ? sxy[0][dy][dx] : (dz == 2 ? sxy[1][dy][dx] : sxy[0][dy][dx] + sxy[1][dy][dx]);
               const int cls = (dx != 1) + 2 * (dy != 1) + 4 * (dz != 1);
-              acc = fma(-(P.Kp[cls] * s), u[i + (dx - 1) + NX * ((dy - 1) + NY * (dz - 1))], acc);
+              t[cls] = fma(s, u[i + (dx - 1) + NX * ((dy - 1) + NY * (dz - 1))], t[cls]);
             }
-        r64[k] = acc;
+        double acc = P.load * 8.0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc = fma(-P.Kp[c], t[c], acc);
+        r[k] = (float)acc;  // scaled below, once the max is known
         amax = fmax(amax, fabs(acc));
       }
-      rnorm = bmax<T>(amax, red);
+      rnorm = bmax<T>(amax, redd);
       if (outer == 0) r0 = rnorm;
       if (!isfinite(rnorm)) { status = MRG_ENUMERIC; break; }
       if (rnorm == 0.0 || rnorm <= A.tol * r0 || outer >= A.max_outer) break;
-      // FP32 Jacobi PCG on J32 d = r (x0 = 0)
-      // Dot products: each thread sums its (at most R) rows in FP32 and converts once; the block sum is
-      // FP64.  (Per-row FP64 accumulation costs a conversion and an add on the FP64 pipe per row and
-      // iteration, which on GB300 runs at 1/64 of the FP32 rate.)
-      float x[R], r[R], z[R];
+      // FP32 Jacobi PCG on J32 d = r / ||r||_inf (x0 = 0): the scaled residual is O(1), so FP32 squares and
+      // dot products stay far from the FP32 range limits whatever the refinement level (r itself is held
+      // in FP32 from here on, as the inner solve is)
+      const float sc = (float)(1.0 / rnorm);
       float rrf = 0.0f, rzf = 0.0f;
 #pragma unroll
       for (int k = 0; k < R; ++k) {
+        if (k >= kn) break;
         const int i = threadIdx.x + k * T;
-        x[k] = 0.0f;
-        r[k] = (float)r64[k];
-        z[k] = r[k] * minv[k];
-        if (i < nn) p_sh[i] = z[k];
+        r[k] *= sc;
+        const float z = r[k] * mi_sh[i];
+        x_sh[i] = 0.0f;
+        p_sh[i] = z;
         rrf = fmaf(r[k], r[k], rrf);
-        rzf = fmaf(r[k], z[k], rzf);
+        rzf = fmaf(r[k], z, rzf);
       }
-      double rr = bsumf<T>(rrf, red);
-      double rho = bsumf<T>(rzf, red);
-      const double stop2 = A.inner_tol * A.inner_tol * rr;  // ||r||^2 threshold of the inner solve
+      float2 d2 = bsum2<T>(rrf, rzf, red, half);
+      float rr = d2.x, rho = d2.y;
+      const float stop2 = (float)A.inner_tol * (float)A.inner_tol * rr;  // ||r||^2 threshold of the inner solve
       int it = 0;
-      while (it < A.max_inner && rr > stop2 && stop2 > 0.0) {
+      while (it < A.max_inner && rr > stop2 && stop2 > 0.0f) {
         // q = J p  (stored FP32 Jacobian rows, p from shared memory)
         float q[R];
         float pqf = 0.0f;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
           q[k] = 0.0f;
+          if (k >= kn) break;
+          if (!((interior >> k) & 1u)) continue;
           const int i = threadIdx.x + k * T;
-          if (i >= nn || !interior[k]) continue;
-          const float* row = J + rp32[k];
+          const float* row = J + rp_sh[i];
           float acc = 0.0f;
 #pragma unroll
           for (int dz = -1; dz <= 1; ++dz)
@@ -301,40 +326,42 @@ __global__ void __launch_bounds__(T) k_batch(const BatchArgs A) {
           q[k] = acc;
           pqf = fmaf(acc, p_sh[i], pqf);
         }
-        const double pq = bsumf<T>(pqf, red);
-        if (!(pq > 0.0)) { status = MRG_ENUMERIC; break; }
-        const float alpha = (float)rho / (float)pq;  // FP32 division (the inner solve is FP32)
+        const float pq = bsum2<T>(pqf, 0.0f, red, half).x;
+        if (!(pq > 0.0f)) { status = MRG_ENUMERIC; break; }
+        const float alpha = rho / pq;
         rrf = 0.0f;
         rzf = 0.0f;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
+          if (k >= kn) break;
           const int i = threadIdx.x + k * T;
-          if (i >= nn) continue;
-          x[k] = fmaf(alpha, p_sh[i], x[k]);
+          x_sh[i] = fmaf(alpha, p_sh[i], x_sh[i]);
           r[k] = fmaf(-alpha, q[k], r[k]);
-          z[k] = r[k] * minv[k];
+          const float z = r[k] * mi_sh[i];
           rrf = fmaf(r[k], r[k], rrf);
-          rzf = fmaf(r[k], z[k], rzf);
+          rzf = fmaf(r[k], z, rzf);
         }
-        rr = bsumf<T>(rrf, red);
-        const double rz = bsumf<T>(rzf, red);
-        const float beta = (float)rz / (float)rho;
-        rho = rz;
+        d2 = bsum2<T>(rrf, rzf, red, half);
+        rr = d2.x;
+        const float beta = d2.y / rho;
+        rho = d2.y;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
+          if (k >= kn) break;
           const int i = threadIdx.x + k * T;
-          if (i < nn) p_sh[i] = fmaf(beta, p_sh[i], z[k]);
+          p_sh[i] = fmaf(beta, p_sh[i], r[k] * mi_sh[i]);
         }
         __syncthreads();
         ++it;
       }
       if (status != MRG_OK) break;
       inner_tot += it;
-      // u += d  (FP64); Dirichlet rows have r = 0 -> d = 0
+      // u += ||r|| x  (FP64); Dirichlet rows have r = 0 -> x = 0
 #pragma unroll
       for (int k = 0; k < R; ++k) {
+        if (k >= kn) break;
         const int i = threadIdx.x + k * T;
-        if (i < nn && interior[k]) u[i] += (double)x[k];
+        if ((interior >> k) & 1u) u[i] = fma((double)x_sh[i], rnorm, u[i]);
       }
       __syncthreads();
       ++outer;
@@ -445,6 +472,11 @@ extern "C" int mrg_batch_create(const mrg_batch_desc* d, mrg_batch** out) {
     return fail(e, "upload kappa32");
   if ((e = cudaMemcpy(B->d_g, d->dirichlet, B->nnode * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
     return fail(e, "upload dirichlet");
+  // four shared-memory arrays of max_nodes words per CTA (78.6 KB for 16^3-cell problems)
+  const int smem = 4 * B->max_nodes * (int)sizeof(float);
+  for (const KCfg& c : kCfgs)
+    if ((e = cudaFuncSetAttribute(c.k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+      return fail(e, "batch kernel shared memory");
   *out = B;
   return MRG_OK;
 }
@@ -489,8 +521,8 @@ static int launch_batch(mrg_batch* B, double* u, float* J, const mrg_batch_opts*
   if (!cfg) return mrg_fail(MRG_EINVAL, "mrg_batch: unsupported thread count");
   if (B->max_nodes > cfg->threads * cfg->rows) return mrg_fail(MRG_EINVAL, "mrg_batch: problem too large for config");
   BatchArgs A{B->d_probs, B->d_order, B->nprob, B->d_kappa, B->d_kappa32, B->d_g, u, J, B->d_counter, B->d_stats,
-              o->tol, o->inner_tol, o->max_outer, o->max_inner};
-  const int smem = B->max_nodes * (int)sizeof(float);
+              o->tol, o->inner_tol, o->max_outer, o->max_inner, B->max_nodes};
+  const int smem = 4 * B->max_nodes * (int)sizeof(float);  // p, x, 1/diag, row offsets
   const int grid = std::max(1, std::min(B->nprob, nsm * ctas_per_sm));
   MRG_CUDA(cudaMemsetAsync(B->d_counter, 0, sizeof(int), s));
   cfg->k<<<grid, cfg->threads, smem, s>>>(A);
