@@ -139,6 +139,52 @@ __device__ __forceinline__ bool is_done(const GScal* S) { return ((volatile cons
 // masked interpolation is a tensor product and P^T A P is three such sweeps (x, then y, then z),
 // each keeping the 27-point layout on an intermediate grid: ~160 multiply-adds per output row instead
 // of ~5,800 for the direct triple product.
+//
+// Rows away from the faces (output index >= 2 from every face, and 2 I + 2 <= nnf - 2 along the swept
+// axis) of a 27-point (p = 1) 3-D sweep take a fast path: every fine column and coarse parent there is
+// free and has the standard weights (1/2, 1, 1/2), so the loops unroll with compile-time accumulator
+// positions (registers instead of a local-memory array).  It adds the same products in the same order
+// as the general loop, so the result is bit-identical.
+template <typename T, int A>
+__device__ __forceinline__ void rap_axis_interior(const Grid& gf, const int I[3], const T* __restrict__ Af,
+                                                  T* __restrict__ out) {
+  T acc[3][3][3];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) (&acc[0][0][0])[k] = T(0);
+#pragma unroll
+  for (int dc = -1; dc <= 1; ++dc) {  // children 2I-1, 2I, 2I+1 along A
+    int f[3] = {I[0], I[1], I[2]};
+    f[A] = 2 * I[A] + dc;
+    const T* vals = Af + row_info<1>(gf, f[0], f[1], f[2]).rp;  // full 27-point row
+    const T wc = (dc == 0) ? T(1) : T(0.5);
+#pragma unroll
+    for (int ez = -1; ez <= 1; ++ez)
+#pragma unroll
+      for (int ey = -1; ey <= 1; ++ey)
+#pragma unroll
+        for (int ex = -1; ex <= 1; ++ex) {
+          const T a = vals[(ez + 1) * 9 + (ey + 1) * 3 + (ex + 1)] * wc;
+          const int e[3] = {ex, ey, ez};
+          const int sft = dc + e[A];  // fine column along A relative to 2I: -2..2
+          int o[3] = {ex, ey, ez};
+          if ((sft & 1) == 0) {
+            o[A] = sft / 2;
+            T& t = acc[o[2] + 1][o[1] + 1][o[0] + 1];
+            t += a * T(1);
+          } else {
+            o[A] = (sft - 1) / 2;
+            T& t0 = acc[o[2] + 1][o[1] + 1][o[0] + 1];
+            t0 += a * T(0.5);
+            o[A] = (sft + 1) / 2;
+            T& t1 = acc[o[2] + 1][o[1] + 1][o[0] + 1];
+            t1 += a * T(0.5);
+          }
+        }
+  }
+#pragma unroll
+  for (int k = 0; k < 27; ++k) out[k] = (&acc[0][0][0])[k];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, P3 pf, Grid gc, P3 pc, int axis, const T* __restrict__ Af,
                                                  T* __restrict__ Ac, int* __restrict__ err) {
@@ -154,6 +200,18 @@ __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, P3 pf, Grid gc, P3 pc,
     const int dg = (int)(diag_pos(Rc, I[0], I[1], I[2]) - Rc.rp);
     for (int e = 0; e < lenc; ++e) out[e] = (e == dg) ? T(1) : T(0);
     return;
+  }
+  if (gf.dim == 3 && pf.p[0] == 1 && pf.p[1] == 1 && pf.p[2] == 1 && pc.p[0] == 1 && pc.p[1] == 1 && pc.p[2] == 1) {
+    bool inner = I[axis] >= 2 && 2 * I[axis] + 2 <= gf.nn[axis] - 2;
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      if (b != axis) inner = inner && I[b] >= 2 && I[b] <= gf.nn[b] - 3;
+    if (inner) {
+      if (axis == 0) rap_axis_interior<T, 0>(gf, I, Af, out);
+      else if (axis == 1) rap_axis_interior<T, 1>(gf, I, Af, out);
+      else rap_axis_interior<T, 2>(gf, I, Af, out);
+      return;
+    }
   }
   constexpr int MAXROW = 75;  // 3 x 5 x 5: the widest output row (one axis swept from a Q2 grid)
   if (lenc > MAXROW) { atomicExch(err, 1); return; }
