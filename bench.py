@@ -523,6 +523,21 @@ def run_profile(args, local_rank):
 
     torch.cuda.set_device(local_rank)
     mrhyde_gb300.load()
+    if args.profile == "c3gmg":  # C3 mixed Newton with p-multigrid BiCGStab: warm-up solve(s), then the solve(s)
+        from mrhyde_gb300 import Problem, SolverManager
+        from mrhyde_gb300.workloads import c3
+
+        cfg, u0 = c3(seed=3, n=args.c3_n)
+        P = Problem(**cfg)
+        S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=25, linear_tol=1e-3, linear_maxiter=20000,
+                          mixed_precision=True, preconditioner="gmg")
+        for _ in range(args.warmup + args.steps):
+            uu = torch.tensor(u0, device="cuda")
+            res = S.nonlinearSolver(uu, raise_on_noconv=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "c3gmg", "steps": args.steps, "newton_iters": res.outer_iterations,
+                          "krylov_iters": res.iterations, "rel_residual_inf": res.rel_residual}))
+        return
     if args.profile == "c4":  # the batched subgrid solve, default configuration (no autotuning)
         from mrhyde_gb300.subgrid import SubgridBatch
         from mrhyde_gb300.workloads import c4_problem, c4_sizes
@@ -588,7 +603,7 @@ def main():
     ap.add_argument("--c3-n", type=int, default=64)
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c4"],
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c3gmg", "c4"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -45,6 +45,7 @@ constexpr double CHEB_LO = 0.25;   // lower end of the smoothed interval, fracti
 constexpr int GCHUNK = 4;          // CG iterations per captured graph
 constexpr int MAXC = 32;           // largest coarsest level solved densely
 constexpr int MAXLEV = 16;
+constexpr int64_t RAP_WARP_ROWS = 24576;  // Galerkin sweeps with fewer output rows: one warp per row
 
 // ---- 1-D transfer along one axis ----------------------------------------------------------------
 // Parents of fine node i (fine nodes 0..nnf-1, coarse nodes 0..nnc-1) with interpolation weights.
@@ -140,49 +141,63 @@ __device__ __forceinline__ bool is_done(const GScal* S) { return ((volatile cons
 // each keeping the 27-point layout on an intermediate grid: ~160 multiply-adds per output row instead
 // of ~5,800 for the direct triple product.
 //
-// Rows away from the faces (output index >= 2 from every face, and 2 I + 2 <= nnf - 2 along the swept
-// axis) of a 27-point (p = 1) 3-D sweep take a fast path: every fine column and coarse parent there is
-// free and has the standard weights (1/2, 1, 1/2), so the loops unroll with compile-time accumulator
-// positions (registers instead of a local-memory array).  It adds the same products in the same order
-// as the general loop, so the result is bit-identical.
-template <typename T, int A>
-__device__ __forceinline__ void rap_axis_interior(const Grid& gf, const int I[3], const T* __restrict__ Af,
-                                                  T* __restrict__ out) {
-  T acc[3][3][3];
+// Rows away from the faces take a fast path: every fine column and coarse parent there is free and has the
+// standard weights (1/2, 1, 1/2), and every row has its full width, so the loops unroll with
+// compile-time accumulator positions (registers instead of a local-memory array).  Row widths along an
+// axis: 3 on a p = 1 axis; on a p = 2 axis 5 at even (vertex) nodes and 3 at odd (mid-edge) nodes.  The
+// swept axis A goes from p = QA ? 2 : 1 to p = 1; the other two axes keep their widths WB, WC (B < C).
+// The fast path adds the same products in the same order as the general loop (children ascending, then
+// the row's entries in storage order, then the lower and upper parent), so the result is bit-identical.
+template <typename T, int A, bool QA, int WB, int WC, int DC>
+__device__ __forceinline__ void rap_child(const Grid& gf, const P3& pf, const int I[3], const T* __restrict__ Af,
+                                          T* acc) {
+  constexpr int B = (A == 0) ? 1 : 0;  // the lower of the two other axes (C is the remaining one)
+  constexpr int WA = (QA && DC == 0) ? 5 : 3;  // child 2I is a vertex node, 2I +- 1 mid-edge nodes
+  constexpr int W0 = (A == 0) ? WA : (B == 0 ? WB : WC);
+  constexpr int W1 = (A == 1) ? WA : (B == 1 ? WB : WC);
+  constexpr int W2 = (A == 2) ? WA : (B == 2 ? WB : WC);
+  constexpr int O0 = (A == 0) ? 3 : W0, O1 = (A == 1) ? 3 : W1, O2 = (A == 2) ? 3 : W2;  // output widths
+  int f[3] = {I[0], I[1], I[2]};
+  f[A] = 2 * I[A] + DC;
+  const T* vals = Af + row_info_p3(gf, pf, f[0], f[1], f[2]).rp;
+  const T wc = (DC == 0) ? T(1) : T(0.5);
 #pragma unroll
-  for (int k = 0; k < 27; ++k) (&acc[0][0][0])[k] = T(0);
+  for (int ez = -(W2 - 1) / 2; ez <= (W2 - 1) / 2; ++ez)
 #pragma unroll
-  for (int dc = -1; dc <= 1; ++dc) {  // children 2I-1, 2I, 2I+1 along A
-    int f[3] = {I[0], I[1], I[2]};
-    f[A] = 2 * I[A] + dc;
-    const T* vals = Af + row_info<1>(gf, f[0], f[1], f[2]).rp;  // full 27-point row
-    const T wc = (dc == 0) ? T(1) : T(0.5);
+    for (int ey = -(W1 - 1) / 2; ey <= (W1 - 1) / 2; ++ey)
 #pragma unroll
-    for (int ez = -1; ez <= 1; ++ez)
-#pragma unroll
-      for (int ey = -1; ey <= 1; ++ey)
-#pragma unroll
-        for (int ex = -1; ex <= 1; ++ex) {
-          const T a = vals[(ez + 1) * 9 + (ey + 1) * 3 + (ex + 1)] * wc;
-          const int e[3] = {ex, ey, ez};
-          const int sft = dc + e[A];  // fine column along A relative to 2I: -2..2
-          int o[3] = {ex, ey, ez};
-          if ((sft & 1) == 0) {
-            o[A] = sft / 2;
-            T& t = acc[o[2] + 1][o[1] + 1][o[0] + 1];
-            t += a * T(1);
-          } else {
-            o[A] = (sft - 1) / 2;
-            T& t0 = acc[o[2] + 1][o[1] + 1][o[0] + 1];
-            t0 += a * T(0.5);
-            o[A] = (sft + 1) / 2;
-            T& t1 = acc[o[2] + 1][o[1] + 1][o[0] + 1];
-            t1 += a * T(0.5);
-          }
+      for (int ex = -(W0 - 1) / 2; ex <= (W0 - 1) / 2; ++ex) {
+        const T a = vals[((ez + (W2 - 1) / 2) * W1 + (ey + (W1 - 1) / 2)) * W0 + (ex + (W0 - 1) / 2)] * wc;
+        const int e[3] = {ex, ey, ez};
+        const int sft = DC + e[A];  // fine column along A relative to 2I: -2..2
+        int o[3] = {ex, ey, ez};
+        if ((sft & 1) == 0) {
+          o[A] = sft / 2;
+          T& t = acc[((o[2] + (O2 - 1) / 2) * O1 + (o[1] + (O1 - 1) / 2)) * O0 + (o[0] + (O0 - 1) / 2)];
+          t += a * T(1);
+        } else {
+          o[A] = (sft - 1) / 2;
+          T& t0 = acc[((o[2] + (O2 - 1) / 2) * O1 + (o[1] + (O1 - 1) / 2)) * O0 + (o[0] + (O0 - 1) / 2)];
+          t0 += a * T(0.5);
+          o[A] = (sft + 1) / 2;
+          T& t1 = acc[((o[2] + (O2 - 1) / 2) * O1 + (o[1] + (O1 - 1) / 2)) * O0 + (o[0] + (O0 - 1) / 2)];
+          t1 += a * T(0.5);
         }
-  }
+      }
+}
+
+template <typename T, int A, bool QA, int WB, int WC>
+__device__ __forceinline__ void rap_interior(const Grid& gf, const P3& pf, const int I[3], const T* __restrict__ Af,
+                                             T* __restrict__ out) {
+  constexpr int LEN = 3 * WB * WC;
+  T acc[LEN];
 #pragma unroll
-  for (int k = 0; k < 27; ++k) out[k] = (&acc[0][0][0])[k];
+  for (int k = 0; k < LEN; ++k) acc[k] = T(0);
+  rap_child<T, A, QA, WB, WC, -1>(gf, pf, I, Af, acc);
+  rap_child<T, A, QA, WB, WC, 0>(gf, pf, I, Af, acc);
+  rap_child<T, A, QA, WB, WC, 1>(gf, pf, I, Af, acc);
+#pragma unroll
+  for (int k = 0; k < LEN; ++k) out[k] = acc[k];
 }
 
 template <typename T>
@@ -201,15 +216,19 @@ __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, P3 pf, Grid gc, P3 pc,
     for (int e = 0; e < lenc; ++e) out[e] = (e == dg) ? T(1) : T(0);
     return;
   }
+  // fast path: 3-D, order 1 throughout (the h-levels).  The same template covers order-2 rows, but
+  // instantiating those variants in this kernel raised it from 64 to 128 (FP32) / 254 (FP64) registers
+  // and slowed every sweep; on the Q2 -> Q1 sweeps it was no faster than the loop below (1.66 vs 1.40 ms
+  // for the first sweep of a 64^3 Q2 grid).
   if (gf.dim == 3 && pf.p[0] == 1 && pf.p[1] == 1 && pf.p[2] == 1 && pc.p[0] == 1 && pc.p[1] == 1 && pc.p[2] == 1) {
     bool inner = I[axis] >= 2 && 2 * I[axis] + 2 <= gf.nn[axis] - 2;
 #pragma unroll
     for (int b = 0; b < 3; ++b)
       if (b != axis) inner = inner && I[b] >= 2 && I[b] <= gf.nn[b] - 3;
     if (inner) {
-      if (axis == 0) rap_axis_interior<T, 0>(gf, I, Af, out);
-      else if (axis == 1) rap_axis_interior<T, 1>(gf, I, Af, out);
-      else rap_axis_interior<T, 2>(gf, I, Af, out);
+      if (axis == 0) rap_interior<T, 0, false, 3, 3>(gf, pf, I, Af, out);
+      else if (axis == 1) rap_interior<T, 1, false, 3, 3>(gf, pf, I, Af, out);
+      else rap_interior<T, 2, false, 3, 3>(gf, pf, I, Af, out);
       return;
     }
   }
@@ -246,6 +265,91 @@ __global__ void __launch_bounds__(NT) k_rap_axis(Grid gf, P3 pf, Grid gc, P3 pc,
         }
   }
   for (int e = 0; e < lenc; ++e) out[e] = acc[e];
+}
+
+// The same sweep with one warp per output row and the lanes over the row's entries: an entry sums, over
+// the children c of the row and the fine columns j whose parent is the entry's column, a_c(j) w_c w_j --
+// the row loop above adds exactly these products, in the same order (children ascending, then fine
+// columns ascending), so the result is bit-identical.  Used on small levels (below ~25k output rows),
+// where one thread's serial walk over a row set the duration of the thread-per-row loop (42 µs for a
+// 128-row level against 8 µs here); above that the thread-per-row fast path is faster.
+// Children of coarse node c along a coarsened axis in three fixed slots (fine 2c-1, 2c, 2c+1): the
+// same set, order and weights as axis_children, without its run-time slot index.
+__device__ __forceinline__ void children3(int c, int nnf, int nnc, int ci[3], float cw[3], bool ok[3]) {
+  ci[0] = 2 * c - 1;
+  ci[1] = 2 * c;
+  ci[2] = 2 * c + 1;
+  // 2c-1 (odd): parents (i-1)/2, (i+1)/2 = c with weight 1/2, or the kept odd last node (parent nnc-1, 1)
+  ok[0] = c >= 1 && ci[0] <= nnf - 1 && (ci[0] != nnf - 1 || c == nnc - 1);
+  cw[0] = (ci[0] == nnf - 1) ? 1.0f : 0.5f;
+  ok[1] = ci[1] <= nnf - 1;  // even: parent c, weight 1
+  cw[1] = 1.0f;
+  ok[2] = ci[2] <= nnf - 2;  // odd, not the last node: parents c and c+1, weight 1/2
+  cw[2] = 0.5f;
+}
+
+template <typename T, int A>
+__global__ void __launch_bounds__(NT) k_rap_axis_w(Grid gf, P3 pf, Grid gc, P3 pc, const T* __restrict__ Af,
+                                                   T* __restrict__ Ac) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 5;
+  const int64_t nrows = (int64_t)gc.nn[0] * gc.nn[1] * gc.nn[2];
+  if (n >= nrows) return;  // uniform over the warp
+  int I[3];
+  decompose(gc, n, I[0], I[1], I[2]);
+  const RowInfo Rc = row_info_p3(gc, pc, I[0], I[1], I[2]);
+  const int lenc = Rc.cx * Rc.cy * Rc.cz;
+  T* out = Ac + Rc.rp;
+  if (node_fixed(gc, I[0], I[1], I[2])) {
+    const int dg = (int)(diag_pos(Rc, I[0], I[1], I[2]) - Rc.rp);
+    for (int e = lane; e < lenc; e += 32) out[e] = (e == dg) ? T(1) : T(0);
+    return;
+  }
+  const int nnf = gf.nn[A], nnc = gc.nn[A];
+  int ci[3];
+  float cw[3];
+  bool cok[3];
+  children3(I[A], nnf, nnc, ci, cw, cok);
+  RowInfo Rf[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    int f[3] = {I[0], I[1], I[2]};
+    f[A] = ci[c];
+    cok[c] = cok[c] && !node_fixed(gf, f[0], f[1], f[2]);
+    if (cok[c]) Rf[c] = row_info_p3(gf, pf, f[0], f[1], f[2]);
+  }
+  for (int e = lane; e < lenc; e += 32) {
+    int o[3];
+    o[0] = Rc.lx + e % Rc.cx;
+    o[1] = Rc.ly + (e / Rc.cx) % Rc.cy;
+    o[2] = Rc.lz + e / (Rc.cx * Rc.cy);
+    T acc = T(0);
+    if (!node_fixed(gc, o[0], o[1], o[2])) {
+      int cj[3];
+      float wj[3];
+      bool jok[3];
+      children3(o[A], nnf, nnc, cj, wj, jok);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (!cok[c]) continue;
+        const RowInfo& R = Rf[c];
+        const T* vals = Af + R.rp;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (!jok[k]) continue;
+          int j[3] = {o[0], o[1], o[2]};
+          j[A] = cj[k];
+          if (j[0] < R.lx || j[0] >= R.lx + R.cx || j[1] < R.ly || j[1] >= R.ly + R.cy || j[2] < R.lz ||
+              j[2] >= R.lz + R.cz)
+            continue;
+          if (node_fixed(gf, j[0], j[1], j[2])) continue;
+          const T a = vals[((j[2] - R.lz) * R.cy + (j[1] - R.ly)) * R.cx + (j[0] - R.lx)] * (T)cw[c];
+          acc += a * (T)wj[k];
+        }
+      }
+    }
+    out[e] = acc;
+  }
 }
 
 // minv = 1 / diag; Gershgorin bound max_i sum_j |a_ij| / |a_ii| into lmax (as float bits, atomicMax)
@@ -970,7 +1074,13 @@ int setup_values(Hier<T>* H, const T* J, cudaStream_t s) {
         const P3 pout = last ? L.pp : L.mid_pp[w];
         T* aout = last ? (T*)L.A : H->mid[w];
         const int64_t nout = (int64_t)gout.nn[0] * gout.nn[1] * gout.nn[2];
-        k_rap_axis<T><<<nblk(nout, NT), NT, 0, s>>>(*gin, pin, gout, pout, L.sweep_axis[w], ain, aout, H->err);
+        if (nout < RAP_WARP_ROWS) {
+          const unsigned nb = nblk(nout * 32, NT);
+          if (L.sweep_axis[w] == 0) k_rap_axis_w<T, 0><<<nb, NT, 0, s>>>(*gin, pin, gout, pout, ain, aout);
+          else if (L.sweep_axis[w] == 1) k_rap_axis_w<T, 1><<<nb, NT, 0, s>>>(*gin, pin, gout, pout, ain, aout);
+          else k_rap_axis_w<T, 2><<<nb, NT, 0, s>>>(*gin, pin, gout, pout, ain, aout);
+        } else
+          k_rap_axis<T><<<nblk(nout, NT), NT, 0, s>>>(*gin, pin, gout, pout, L.sweep_axis[w], ain, aout, H->err);
         MRG_CUDA(cudaGetLastError());
         gin = &gout;
         pin = pout;
