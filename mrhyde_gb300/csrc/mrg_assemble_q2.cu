@@ -34,7 +34,26 @@ struct TPTabs {
   double W[27];       // w_q * |detJ|
   double s[3];        // 2 / h_d
   double load[27];    // f * sum_q W_q phi_l(q)
+  float phi1f[3][3], dph1f[3][3], Wf[27], sf[3];  // FP32 copies for the FP32 coefficient pass
 };
+
+// table access in the pass's arithmetic type
+template <typename CT>
+__device__ __forceinline__ CT tp_phi(const TPTabs& T, int q, int a) {
+  if constexpr (sizeof(CT) == 4) return T.phi1f[q][a]; else return T.phi1[q][a];
+}
+template <typename CT>
+__device__ __forceinline__ CT tp_dph(const TPTabs& T, int q, int a) {
+  if constexpr (sizeof(CT) == 4) return T.dph1f[q][a]; else return T.dph1[q][a];
+}
+template <typename CT>
+__device__ __forceinline__ CT tp_w(const TPTabs& T, int q) {
+  if constexpr (sizeof(CT) == 4) return T.Wf[q]; else return T.W[q];
+}
+template <typename CT>
+__device__ __forceinline__ CT tp_s(const TPTabs& T, int d) {
+  if constexpr (sizeof(CT) == 4) return T.sf[d]; else return T.s[d];
+}
 
 template <int P>
 struct TP {
@@ -61,15 +80,18 @@ __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float(r);
 }
 
-// mode bits: 1 = scatter residual, 2 = store qp coefficients (QT precision)
-template <int P, typename QT>
+// mode bits: 1 = scatter residual, 2 = store qp coefficients (QT precision).  CT = arithmetic type of
+// the interpolation stages: double for every pass that scatters the residual; float for the pass that
+// only stores the FP32 coefficients of the FP32 Jacobian (1 + u^2 and 2 u grad u at the Gauss points),
+// which the FP64 stages made FP64-pipe bound (~1,000 FP64 operations a cell).
+template <int P, typename QT, typename CT = double>
 __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int color, int cc0, int cc1, int64_t ncl,
                                                     int kind, const double* __restrict__ u,
                                                     const double* __restrict__ kap, double* __restrict__ r,
                                                     QT* __restrict__ qbuf, int tc_image, int mode) {
   using K = TP<P>;
   constexpr int N1 = K::N1, NL = K::NL;
-  __shared__ double sm[RW][K::CPW][6][NL];
+  __shared__ CT sm[RW][K::CPW][6][NL];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / NL, l = lane % NL;
   const int64_t cl = ((int64_t)blockIdx.x * RW + w) * K::CPW + sub;
@@ -95,27 +117,27 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
   int i0 = 0, i1 = 0, i2 = 0;
   split3(l, N1, i0, i1, i2);
   const int sc = on ? sub : 0;
-  double* U = sm[w][sc][0];
-  double* X0 = sm[w][sc][1];
-  double* X1 = sm[w][sc][2];
-  double* Y0 = sm[w][sc][3];
-  double* Y1 = sm[w][sc][4];
-  double* Y2 = sm[w][sc][5];
+  CT* U = sm[w][sc][0];
+  CT* X0 = sm[w][sc][1];
+  CT* X1 = sm[w][sc][2];
+  CT* Y0 = sm[w][sc][3];
+  CT* Y1 = sm[w][sc][4];
+  CT* Y2 = sm[w][sc][5];
   const int NX = g.nn[0], NY = g.nn[1];
   int64_t node = 0;
   if (on) {
     node = (P * cx + i0) + (int64_t)NX * ((P * cy + i1) + (int64_t)NY * (P * cz + i2));
-    U[l] = __ldg(u + node);
+    U[l] = (CT)__ldg(u + node);
   }
   __syncwarp();
   // stage x: lane (qx,b,c)
   if (on) {
-    double a0 = 0.0, a1 = 0.0;
+    CT a0 = CT(0), a1 = CT(0);
 #pragma unroll
     for (int a = 0; a < N1; ++a) {
-      const double v = U[a + N1 * i1 + N1 * N1 * i2];
-      a0 = fma(T.phi1[i0][a], v, a0);
-      a1 = fma(T.dph1[i0][a], v, a1);
+      const CT v = U[a + N1 * i1 + N1 * N1 * i2];
+      a0 = fma(tp_phi<CT>(T, i0, a), v, a0);
+      a1 = fma(tp_dph<CT>(T, i0, a), v, a1);
     }
     X0[l] = a0;
     X1[l] = a1;
@@ -123,13 +145,13 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
   __syncwarp();
   // stage y: lane (qx,qy,c)
   if (on) {
-    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    CT b0 = CT(0), b1 = CT(0), b2 = CT(0);
 #pragma unroll
     for (int b = 0; b < N1; ++b) {
-      const double ux = X0[i0 + N1 * b + N1 * N1 * i2], dx = X1[i0 + N1 * b + N1 * N1 * i2];
-      b0 = fma(T.phi1[i1][b], ux, b0);
-      b1 = fma(T.phi1[i1][b], dx, b1);
-      b2 = fma(T.dph1[i1][b], ux, b2);
+      const CT ux = X0[i0 + N1 * b + N1 * N1 * i2], dx = X1[i0 + N1 * b + N1 * N1 * i2];
+      b0 = fma(tp_phi<CT>(T, i1, b), ux, b0);
+      b1 = fma(tp_phi<CT>(T, i1, b), dx, b1);
+      b2 = fma(tp_dph<CT>(T, i1, b), ux, b2);
     }
     Y0[l] = b0;
     Y1[l] = b1;
@@ -137,29 +159,29 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
   }
   __syncwarp();
   // stage z: lane = Gauss point q; pointwise flux
-  double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+  CT Fx = CT(0), Fy = CT(0), Fz = CT(0);
   if (on) {
-    double uq = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+    CT uq = CT(0), gx = CT(0), gy = CT(0), gz = CT(0);
 #pragma unroll
     for (int c = 0; c < N1; ++c) {
       const int k = i0 + N1 * i1 + N1 * N1 * c;
-      uq = fma(T.phi1[i2][c], Y0[k], uq);
-      gx = fma(T.phi1[i2][c], Y1[k], gx);
-      gy = fma(T.phi1[i2][c], Y2[k], gy);
-      gz = fma(T.dph1[i2][c], Y0[k], gz);
+      uq = fma(tp_phi<CT>(T, i2, c), Y0[k], uq);
+      gx = fma(tp_phi<CT>(T, i2, c), Y1[k], gx);
+      gy = fma(tp_phi<CT>(T, i2, c), Y2[k], gy);
+      gz = fma(tp_dph<CT>(T, i2, c), Y0[k], gz);
     }
-    const double Wq = T.W[l];
-    const double diff = (kind == MRG_THERMAL) ? __ldg(kap + cid) : 1.0 + uq * uq;
-    const double cw = Wq * diff;
-    Fx = cw * T.s[0] * T.s[0] * gx;
-    Fy = cw * T.s[1] * T.s[1] * gy;
-    Fz = cw * T.s[2] * T.s[2] * gz;
+    const CT Wq = tp_w<CT>(T, l);
+    const CT diff = (kind == MRG_THERMAL) ? (CT)__ldg(kap + cid) : CT(1) + uq * uq;
+    const CT cw = Wq * diff;
+    Fx = cw * tp_s<CT>(T, 0) * tp_s<CT>(T, 0) * gx;
+    Fy = cw * tp_s<CT>(T, 1) * tp_s<CT>(T, 1) * gy;
+    Fz = cw * tp_s<CT>(T, 2) * tp_s<CT>(T, 2) * gz;
     if (mode & 2) {
       QT* qb = qbuf + cid * K::NQB;
       // tc_image (FP32 only): split x = hi + lo (hi = x rounded to TF32, lo = the FP32 remainder rounded to
       // TF32) and store both into the tensor-core operand image [tile][hi, lo][K chunk][cell][4] with
       // 128-cell tiles and 112 K slots; otherwise plain QT values [cell][4 NL]
-      auto put = [&](int k, double v) {
+      auto put = [&](int k, CT v) {
         if constexpr (sizeof(QT) == 4) {
           if (tc_image) {
             // split of the FP32 value (the remainder is exact in FP32; 3xTF32 keeps ~22 bits anyway):
@@ -176,10 +198,10 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
       };
       put(l, cw);
       if (kind != MRG_THERMAL) {
-        const double e = Wq * 2.0 * uq;
-        put(NL + l, e * T.s[0] * T.s[0] * gx);
-        put(2 * NL + l, e * T.s[1] * T.s[1] * gy);
-        put(3 * NL + l, e * T.s[2] * T.s[2] * gz);
+        const CT e = Wq * CT(2) * uq;
+        put(NL + l, e * tp_s<CT>(T, 0) * tp_s<CT>(T, 0) * gx);
+        put(2 * NL + l, e * tp_s<CT>(T, 1) * tp_s<CT>(T, 1) * gy);
+        put(3 * NL + l, e * tp_s<CT>(T, 2) * tp_s<CT>(T, 2) * gz);
       }
     }
   }
@@ -192,14 +214,14 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
   }
   __syncwarp();
   // transpose z: lane (qx,qy,c)
-  double Ax = 0.0, Ay = 0.0, Az = 0.0;
+  CT Ax = CT(0), Ay = CT(0), Az = CT(0);
   if (on) {
 #pragma unroll
     for (int qz = 0; qz < N1; ++qz) {
       const int k = i0 + N1 * i1 + N1 * N1 * qz;
-      Ax = fma(T.phi1[qz][i2], X0[k], Ax);
-      Ay = fma(T.phi1[qz][i2], X1[k], Ay);
-      Az = fma(T.dph1[qz][i2], Y0[k], Az);
+      Ax = fma(tp_phi<CT>(T, qz, i2), X0[k], Ax);
+      Ay = fma(tp_phi<CT>(T, qz, i2), X1[k], Ay);
+      Az = fma(tp_dph<CT>(T, qz, i2), Y0[k], Az);
     }
   }
   __syncwarp();
@@ -210,14 +232,14 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
   }
   __syncwarp();
   // transpose y: lane (qx,b,c)
-  double Bx = 0.0, Byz = 0.0;
+  CT Bx = CT(0), Byz = CT(0);
   if (on) {
 #pragma unroll
     for (int qy = 0; qy < N1; ++qy) {
       const int k = i0 + N1 * qy + N1 * N1 * i2;
-      Bx = fma(T.phi1[qy][i1], Y1[k], Bx);
-      Byz = fma(T.dph1[qy][i1], Y2[k], Byz);
-      Byz = fma(T.phi1[qy][i1], U[k], Byz);
+      Bx = fma(tp_phi<CT>(T, qy, i1), Y1[k], Bx);
+      Byz = fma(tp_dph<CT>(T, qy, i1), Y2[k], Byz);
+      Byz = fma(tp_phi<CT>(T, qy, i1), U[k], Byz);
     }
   }
   __syncwarp();
@@ -228,12 +250,12 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
   __syncwarp();
   // transpose x: lane (a,b,c) = element row
   if (on) {
-    double res = -T.load[l];
+    CT res = (CT)(-T.load[l]);
 #pragma unroll
     for (int qx = 0; qx < N1; ++qx) {
       const int k = qx + N1 * i1 + N1 * N1 * i2;
-      res = fma(T.dph1[qx][i0], X0[k], res);
-      res = fma(T.phi1[qx][i0], X1[k], res);
+      res = fma(tp_dph<CT>(T, qx, i0), X0[k], res);
+      res = fma(tp_phi<CT>(T, qx, i0), X1[k], res);
     }
     if (!node_fixed(g, P * cx + i0, P * cy + i1, P * cz + i2)) r[node] -= res;  // r += -res.val()
   }
@@ -436,6 +458,13 @@ int mrg_q2_setup(mrg_problem* p) {
     Q->T.s[d] = 2.0 / p->h[d];
   }
   for (int q = 0; q < 27; ++q) Q->T.W[q] = (q < nq) ? tw[q] * detJ : 0.0;
+  for (int q = 0; q < 3; ++q)
+    for (int a = 0; a < 3; ++a) {
+      Q->T.phi1f[q][a] = (float)Q->T.phi1[q][a];
+      Q->T.dph1f[q][a] = (float)Q->T.dph1[q][a];
+    }
+  for (int q = 0; q < 27; ++q) Q->T.Wf[q] = (float)Q->T.W[q];
+  for (int d = 0; d < 3; ++d) Q->T.sf[d] = (float)Q->T.s[d];
   for (int l = 0; l < 27; ++l) {
     double s = 0.0;
     if (l < npe)
@@ -482,7 +511,10 @@ static int launch_res_t(mrg_problem* p, const double* u, double* r, void* qbuf, 
   const Grid& g = p->g;
   constexpr int CPB = RW * TP<P>::CPW;  // cells per CTA
   auto launch = [&](int color, int cc0, int cc1, int64_t tot) {
-    if (fp32q)
+    if (fp32q && !(mode & 1))
+      k_tp_res<P, float, float><<<nblk(tot, CPB), RW * 32, 0, s>>>(Q->T, g, color, cc0, cc1, tot, p->kind, u,
+                                                                    p->d_kappa, r, (float*)qbuf, tc_image ? 1 : 0, mode);
+    else if (fp32q)
       k_tp_res<P, float><<<nblk(tot, CPB), RW * 32, 0, s>>>(Q->T, g, color, cc0, cc1, tot, p->kind, u, p->d_kappa, r,
                                                              (float*)qbuf, tc_image ? 1 : 0, mode);
     else
