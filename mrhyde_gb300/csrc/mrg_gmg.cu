@@ -376,14 +376,17 @@ __global__ void __launch_bounds__(NT) k_diag(Grid g, const T* __restrict__ A, T*
   if ((threadIdx.x & 31) == 0 && v > 0.0f) atomicMax(lmax_bits, __float_as_uint(v));
 }
 
-// Dense inverse of the coarsest operator (n <= MAXC), Gauss-Jordan with partial pivoting, one CTA.
+// Dense inverse of the coarsest operator (n <= MAXC), Gauss-Jordan with partial pivoting, one CTA, in
+// the hierarchy's precision (FP32 for the inner solve's hierarchy: FP64 arithmetic there cost the FP64
+// pipe's latency on every step for a preconditioner that is FP32 anyway).  The pivot is the first row
+// of largest magnitude, found by warp 0 with shuffles.
 template <typename T>
 __global__ void __launch_bounds__(NT) k_coarse_inv(Grid g, const T* __restrict__ A, T* __restrict__ inv,
                                                    int* __restrict__ err) {
-  __shared__ double M[MAXC][2 * MAXC];
+  __shared__ T M[MAXC][2 * MAXC];
   __shared__ int piv;
   const int n = g.nn[0] * g.nn[1] * g.nn[2];
-  for (int k = threadIdx.x; k < MAXC * 2 * MAXC; k += NT) (&M[0][0])[k] = 0.0;
+  for (int k = threadIdx.x; k < MAXC * 2 * MAXC; k += NT) (&M[0][0])[k] = T(0);
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += NT) {
     int ix, iy, iz;
@@ -393,28 +396,39 @@ __global__ void __launch_bounds__(NT) k_coarse_inv(Grid g, const T* __restrict__
     for (int jz = R.lz; jz < R.lz + R.cz; ++jz)
       for (int jy = R.ly; jy < R.ly + R.cy; ++jy)
         for (int jx = R.lx; jx < R.lx + R.cx; ++jx, ++e)
-          M[i][jx + g.nn[0] * (jy + g.nn[1] * jz)] = (double)A[R.rp + e];
-    M[i][n + i] = 1.0;
+          M[i][jx + g.nn[0] * (jy + g.nn[1] * jz)] = A[R.rp + e];
+    M[i][n + i] = T(1);
   }
   __syncthreads();
   for (int c = 0; c < n; ++c) {
-    if (threadIdx.x == 0) {
-      int best = c;
-      for (int r = c + 1; r < n; ++r)
-        if (fabs(M[r][c]) > fabs(M[best][c])) best = r;
-      piv = best;
-      if (!(fabs(M[best][c]) > 0.0)) atomicExch(err, 2);
+    if (threadIdx.x < 32) {
+      const int r = threadIdx.x;
+      T v = (r >= c && r < n) ? fabs(M[r][c]) : T(-1);
+      int bi = r;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, v, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ov > v || (ov == v && oi < bi)) {
+          v = ov;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        piv = bi;
+        if (!(v > T(0))) atomicExch(err, 2);
+      }
     }
     __syncthreads();
     const int pr = piv;
     if (pr != c)
       for (int k = threadIdx.x; k < 2 * n; k += NT) {
-        const double t = M[c][k];
+        const T t = M[c][k];
         M[c][k] = M[pr][k];
         M[pr][k] = t;
       }
     __syncthreads();
-    const double inv_p = 1.0 / M[c][c];
+    const T inv_p = T(1) / M[c][c];
     __syncthreads();
     for (int k = threadIdx.x; k < 2 * n; k += NT) M[c][k] *= inv_p;
     __syncthreads();
@@ -424,10 +438,10 @@ __global__ void __launch_bounds__(NT) k_coarse_inv(Grid g, const T* __restrict__
     }
     __syncthreads();
     for (int r = threadIdx.x; r < n; r += NT)
-      if (r != c) M[r][c] = 0.0;
+      if (r != c) M[r][c] = T(0);
     __syncthreads();
   }
-  for (int idx = threadIdx.x; idx < n * n; idx += NT) inv[idx] = (T)M[idx / n][n + idx % n];
+  for (int idx = threadIdx.x; idx < n * n; idx += NT) inv[idx] = M[idx / n][n + idx % n];
 }
 
 // ---- cycle kernels --------------------------------------------------------------------------------
