@@ -295,7 +295,9 @@ def run_ours(args, rank, world, local_rank):
     algo32 = algorithmic_bytes(cells, info.n_dofs, info.nnz, 4)
     ach64 = algo64 / (ms_step * 1e-3) / 1e9
     traffic = read_profile_traffic("k_fact_hex_fp64_c2_128")
-    dp_ops = 73 * (info.n_dofs - info.n_fixed)  # FP64 instructions per launch (19 DADD + 27 DMUL + 27 DFMA per free row)
+    # FP64 instructions per launch: 27 DMUL (K(off) * S(off)) + 27 DFMA (residual) per free row; the kappa
+    # sums are exact fixed-point sums on the integer pipes (19 DADD more per row with MRG_ASM_NATIVE_FP64)
+    dp_ops = 54 * (info.n_dofs - info.n_fixed)
     import ctypes
 
     from mrhyde_gb300 import _lib as LL

@@ -33,6 +33,7 @@ MRG_ASM_ADJOINT = 1024
 MRG_ASM_SENS = 2048
 MRG_ASM_TENSOR_CORES = 4096
 MRG_ASM_CUDA_CORES = 8192
+MRG_ASM_NATIVE_FP64 = 16384
 MRG_NOALLOC_MAX_DOFS = 1 << 18
 
 

@@ -193,10 +193,12 @@ class AssemblyManager:
 
     def assembleJacRes(self, u, res, J, compute_jacobian=True, fp32_jacobian=False, overwrite=False,
                        compute_sens=False, is_adjoint=False, fix_zero_rows=False, force_cell=False, atomic=False,
-                       stream=None, tensor_cores=None):
+                       stream=None, tensor_cores=None, native_fp64=False):
         """r += -res.val(), J += res.dx(); Dirichlet rows skipped, then J(d,d) = 1.
 
         ``overwrite=True`` fuses the caller's ``J.setAllToScalar(0); r.putScalar(0)``.
+        ``native_fp64=True`` forms the factored path's kappa sums with FP64 additions instead of exact
+        fixed-point sums rounded once to FP64 (the default).
         """
         flags = L.MRG_ASM_RES
         if compute_jacobian:
@@ -213,6 +215,8 @@ class AssemblyManager:
             flags |= L.MRG_ASM_ATOMIC
         if tensor_cores is not None:  # Q2 FP32 Jacobians use the tensor cores unless told otherwise
             flags |= L.MRG_ASM_TENSOR_CORES if tensor_cores else L.MRG_ASM_CUDA_CORES
+        if native_fp64:
+            flags |= L.MRG_ASM_NATIVE_FP64
         if compute_sens:
             flags |= L.MRG_ASM_SENS
         if is_adjoint:
@@ -232,8 +236,9 @@ class AssemblyManager:
         L.check(L.lib().mrg_assemble(self.problem.handle, _ptr(u), None, _ptr(J), flags, _stream(stream)),
                 "mrg_assemble")
 
-    def assembleRes(self, u, res, overwrite=False, force_cell=False, atomic=False, stream=None):
+    def assembleRes(self, u, res, overwrite=False, force_cell=False, atomic=False, stream=None, native_fp64=False):
         flags = L.MRG_ASM_RES | (L.MRG_ASM_OVERWRITE if overwrite else 0)
+        flags |= L.MRG_ASM_NATIVE_FP64 if native_fp64 else 0
         flags |= (L.MRG_ASM_FORCE_CELL if force_cell else 0) | (L.MRG_ASM_ATOMIC if atomic else 0)
         self._check_args(u, res, None, True, False, False)
         L.check(L.lib().mrg_assemble(self.problem.handle, _ptr(u), _ptr(res), None, flags, _stream(stream)),

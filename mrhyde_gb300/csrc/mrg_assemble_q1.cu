@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdio>
 
+#include "mrg_fixmul.cuh"
 #include "mrg_internal.h"
 
 namespace {
@@ -104,6 +105,7 @@ struct FactArgs {
   double amp;
   const double* B[3];
   int64_t nrows, nnz;
+  int fixed;          // 1: exact fixed-point kappa sums (mrg_fixmul.cuh) where a row's kappa allow; 0: FP64 additions
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -162,9 +164,11 @@ __global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double*
       }
       if (DOR && OVW) r[n] = 0.0;
     } else {
-      // kappa of the 8 cells around the node (0 outside the mesh)
-      double k[2][2][2];
+      // kappa of the 8 cells around the node (0 outside the mesh), as FP64 bit patterns
+      uint64_t kb[2][2][2];
       float k32[2][2][2];
+      int emax = 0;
+      bool fx = A.fixed;
 #pragma unroll
       for (int c = 0; c < 2; ++c)
 #pragma unroll
@@ -174,35 +178,99 @@ __global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double*
             int ccx = ix - 1 + a, ccy = iy - 1 + b, ccz = iz - 1 + c;
             bool ok = ccx >= 0 && ccx < nx && ccy >= 0 && ccy < ny && ccz >= 0 && ccz < nz;
             int64_t cid = ccx + (int64_t)nx * (ccy + (int64_t)ny * ccz);
-            k[c][b][a] = ok ? __ldg(kap + cid) : 0.0;
+            const uint64_t v = ok ? (uint64_t)__double_as_longlong(__ldg(kap + cid)) : 0ull;
+            kb[c][b][a] = v;
             if (MIXED && DOJ) k32[c][b][a] = ok ? __ldg(kap32 + cid) : 0.0f;
+            if (v) {
+              const int e = (int)(v >> 52);  // sign bit included: a negative kappa gives e > 0x7ff
+              fx = fx && e > 0 && e < 0x7ff;  // positive, normal, finite
+              emax = max(emax, e & 0x7ff);
+            }
           }
-      // separable sums: S[dz][dy][dx] = sum of kappa over the cells shared by node and node+off
-      double sx[2][2][3], sxy[2][3][3], S[3][3][3];
+      fx = fx && emax >= 60;  // rounded sums are normal numbers
+      // S[dz][dy][dx] = sum of kappa over the cells shared by node and node+off
+      double S[3][3][3];
+      if (fx) {
+        // exact sums in the row's 64-bit fixed point (mrg_fixmul.cuh), each rounded once to FP64; the 8
+        // corner entries are single kappa
+        uint64_t kf[2][2][2];
 #pragma unroll
-      for (int c = 0; c < 2; ++c)
+        for (int c = 0; c < 2; ++c)
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-          sx[c][b][0] = k[c][b][0];
-          sx[c][b][1] = k[c][b][0] + k[c][b][1];
-          sx[c][b][2] = k[c][b][1];
-        }
+          for (int b = 0; b < 2; ++b)
 #pragma unroll
-      for (int c = 0; c < 2; ++c)
+            for (int a = 0; a < 2; ++a) {
+              const uint64_t v = kb[c][b][a];
+              const int d = emax - (int)((v >> 52) & 0x7ff);
+              fx = fx && (v == 0 || d <= 7);  // exact in the row's fixed point
+              kf[c][b][a] = v ? ((v & 0x000fffffffffffffull) | 0x0010000000000000ull) << (7 - min(d, 7)) : 0ull;
+            }
+        uint64_t qx[2][2][3], qxy[2][3][3];
 #pragma unroll
-        for (int x = 0; x < 3; ++x) {
-          sxy[c][0][x] = sx[c][0][x];
-          sxy[c][1][x] = sx[c][0][x] + sx[c][1][x];
-          sxy[c][2][x] = sx[c][1][x];
-        }
+        for (int c = 0; c < 2; ++c)
 #pragma unroll
-      for (int y = 0; y < 3; ++y)
+          for (int b = 0; b < 2; ++b) {
+            qx[c][b][0] = kf[c][b][0];
+            qx[c][b][1] = kf[c][b][0] + kf[c][b][1];
+            qx[c][b][2] = kf[c][b][1];
+          }
 #pragma unroll
-        for (int x = 0; x < 3; ++x) {
-          S[0][y][x] = sxy[0][y][x];
-          S[1][y][x] = sxy[0][y][x] + sxy[1][y][x];
-          S[2][y][x] = sxy[1][y][x];
-        }
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int x = 0; x < 3; ++x) {
+            qxy[c][0][x] = qx[c][0][x];
+            qxy[c][1][x] = qx[c][0][x] + qx[c][1][x];
+            qxy[c][2][x] = qx[c][1][x];
+          }
+#pragma unroll
+        for (int z = 0; z < 3; ++z)
+#pragma unroll
+          for (int y = 0; y < 3; ++y)
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+              if (z != 1 && y != 1 && x != 1) {
+                S[z][y][x] = __longlong_as_double((long long)kb[z >> 1][y >> 1][x >> 1]);
+              } else {
+                const uint64_t q = (z == 0) ? qxy[0][y][x] : (z == 2 ? qxy[1][y][x] : qxy[0][y][x] + qxy[1][y][x]);
+                S[z][y][x] = __longlong_as_double((long long)mrgfix::fix_to_f64_bits(q, emax));
+              }
+            }
+      }
+      if (!fx) {
+        // FP64 additions (rows the fixed point does not cover, or MRG_ASM_NATIVE_FP64)
+        double k[2][2][2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int a = 0; a < 2; ++a) k[c][b][a] = __longlong_as_double((long long)kb[c][b][a]);
+        double sx[2][2][3], sxy[2][3][3];
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int b = 0; b < 2; ++b) {
+            sx[c][b][0] = k[c][b][0];
+            sx[c][b][1] = k[c][b][0] + k[c][b][1];
+            sx[c][b][2] = k[c][b][1];
+          }
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int x = 0; x < 3; ++x) {
+            sxy[c][0][x] = sx[c][0][x];
+            sxy[c][1][x] = sx[c][0][x] + sx[c][1][x];
+            sxy[c][2][x] = sx[c][1][x];
+          }
+#pragma unroll
+        for (int y = 0; y < 3; ++y)
+#pragma unroll
+          for (int x = 0; x < 3; ++x) {
+            S[0][y][x] = sxy[0][y][x];
+            S[1][y][x] = sxy[0][y][x] + sxy[1][y][x];
+            S[2][y][x] = sxy[1][y][x];
+          }
+      }
       float S32[3][3][3];
       if (MIXED && DOJ) {
         float tx[2][2][3], txy[2][3][3];
@@ -232,10 +300,9 @@ __global__ void __launch_bounds__(FT) k_fact_hex(const FactArgs A, const double*
           }
       }
       // load vector entry b_i
-      double b;
-      if (A.src_sin) b = A.amp * A.B[0][ix] * A.B[1][iy] * A.B[2][iz];
-      else b = A.loadk[(cx == 3) + (cy == 3) + (cz == 3)];
-      double acc = b;
+      double acc;
+      if (A.src_sin) acc = A.amp * A.B[0][ix] * A.B[1][iy] * A.B[2][iz];
+      else acc = A.loadk[(cx == 3) + (cy == 3) + (cz == 3)];
       double t[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) t[c] = 0.0;
@@ -761,6 +828,7 @@ int mrg_launch_factored(mrg_problem* p, const double* u, double* r, void* J, uin
   A.amp = p->source_amp;
   A.load = p->source_amp * p->cell_load;
   for (int k = 0; k < 4; ++k) A.loadk[k] = std::ldexp(A.load, k);  // exact: a power-of-two scaling
+  A.fixed = (flags & MRG_ASM_NATIVE_FP64) ? 0 : 1;
   if (A.src_sin) {
     A.B[0] = p->d_srcB;
     A.B[1] = p->d_srcB + p->g.nn[0];

@@ -1,0 +1,150 @@
+"""Q1 factored path with exact kappa sums (64-bit fixed point on the integer pipes, each sum rounded once to
+FP64; products and residual FMAs in FP64) against the same path with FP64 additions (MRG_ASM_NATIVE_FP64)
+and against the oracle.
+
+* integer-valued kappa: every kappa sum is exact in FP64 as well, so both paths form the same sums and
+  products -- identical bits;
+* lognormal kappa: the exact sums are rounded once where FP64 rounds every partial sum; entries agree to
+  a few units in the last place (scaled bound 1e-15), residuals within 1e-13 (scaled), both within 1e-12
+  of the oracle;
+* rows whose kappa span more than 2^7, or hold a negative kappa, take the FP64 instructions: identical bits.
+"""
+import numpy as np
+import pytest
+import torch
+
+from tests.cases import gpu_problem, oracle_problem
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+def scaled_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m = np.max(np.abs(b)) if b.size else 1.0
+    scale = np.maximum(np.abs(b), 1e-3 * m)
+    scale[scale == 0] = 1.0
+    return float(np.max(np.abs(a - b) / scale))
+
+
+def _cfg(kappa, n=(9, 7, 6), hi=(1.0, 1.0, 1.0), faces=1 | 2):
+    return dict(dim=3, order=1, n=n, hi=hi, kappa=kappa, dirichlet_faces=faces, source=("const", 1.0, 0.0))
+
+
+def _assemble(G, u, native, fp32=False, jac=True):
+    from mrhyde_gb300 import AssemblyManager
+
+    A = AssemblyManager(G)
+    ud = torch.tensor(u, device="cuda")
+    r = torch.zeros(G.info.n_dofs, dtype=torch.float64, device="cuda")
+    J = torch.zeros(G.info.nnz, dtype=torch.float32 if fp32 else torch.float64, device="cuda")
+    if jac:
+        A.assembleJacRes(ud, r, J, fp32_jacobian=fp32, overwrite=True, native_fp64=native)
+    else:
+        A.assembleRes(ud, r, overwrite=True, native_fp64=native)
+    torch.cuda.synchronize()
+    return r.cpu().numpy(), J.cpu().numpy()
+
+
+def _u(G, seed):
+    return np.random.default_rng(seed).uniform(-1, 1, G.info.n_dofs)
+
+
+@pytest.mark.parametrize("hi", [(1.0, 1.0, 1.0), (1.0, 0.37, 2.5)])
+def test_integer_kappa_bit_identical(hi):
+    n = (9, 7, 6)
+    kap = np.random.default_rng(1).integers(1, 9, n[0] * n[1] * n[2]).astype(np.float64)
+    G = gpu_problem(_cfg(kap, n, hi))
+    u = _u(G, 2)
+    _, J_fx = _assemble(G, u, native=False)
+    _, J_nat = _assemble(G, u, native=True)
+    assert np.array_equal(J_fx.view(np.uint64), J_nat.view(np.uint64))
+
+
+@pytest.mark.parametrize("sigma", [0.5, 1.0])
+def test_lognormal_kappa_within_ulps_and_oracle(sigma):
+    n = (10, 9, 8)
+    kap = np.exp(sigma * np.random.default_rng(3).standard_normal(n[0] * n[1] * n[2]))
+    cfg = _cfg(kap, n)
+    G = gpu_problem(cfg)
+    u = _u(G, 4)
+    r_fx, J_fx = _assemble(G, u, native=False)
+    r_nat, J_nat = _assemble(G, u, native=True)
+    assert scaled_err(J_fx, J_nat) <= 1e-15
+    assert scaled_err(r_fx, r_nat) <= 1e-13
+    r_o, J_o = oracle_problem(cfg).assemble(u)
+    assert scaled_err(J_fx, J_o) <= TOL64
+    assert scaled_err(r_fx, r_o) <= TOL64
+    # residual-only pass forms the same entries in the same order
+    r_r, _ = _assemble(G, u, native=False, jac=False)
+    assert np.array_equal(r_r, r_fx)
+
+
+def _fallback_rows(kap, n):
+    """Rows whose surrounding cells hold a negative kappa or nonzero kappa more than 2^7 apart (binary
+    exponents differing by more than 7)."""
+    nx, ny, nz = n
+    K = kap.reshape(nz, ny, nx)
+    E = np.frexp(np.abs(K))[1]
+    rows = []
+    for iz in range(nz + 1):
+        for iy in range(ny + 1):
+            for ix in range(nx + 1):
+                cz = [c for c in (iz - 1, iz) if 0 <= c < nz]
+                cy = [c for c in (iy - 1, iy) if 0 <= c < ny]
+                cx = [c for c in (ix - 1, ix) if 0 <= c < nx]
+                v = K[np.ix_(cz, cy, cx)].ravel()
+                e = E[np.ix_(cz, cy, cx)].ravel()
+                if (v < 0).any() or e.max() - e.min() > 7:
+                    rows.append(ix + (nx + 1) * (iy + (ny + 1) * iz))
+    return rows
+
+
+@pytest.mark.parametrize("spoil", ["wide", "negative"])
+def test_fallback_rows_bit_identical(spoil):
+    n = (6, 6, 6)
+    kap = np.exp(0.3 * np.random.default_rng(5).standard_normal(n[0] * n[1] * n[2]))
+    if spoil == "wide":
+        kap[::7] *= 1e3   # neighbouring kappa ~2^10 apart: those rows take the FP64 instructions
+    else:
+        kap[11] = -0.5
+    G = gpu_problem(_cfg(kap, n))
+    u = _u(G, 6)
+    r_fx, J_fx = _assemble(G, u, native=False)
+    r_nat, J_nat = _assemble(G, u, native=True)
+    rp, _ = G.graph()
+    rp = rp.cpu().numpy()
+    fb = _fallback_rows(kap, n)
+    assert fb
+    for row in fb:
+        assert np.array_equal(J_fx[rp[row]:rp[row + 1]].view(np.uint64), J_nat[rp[row]:rp[row + 1]].view(np.uint64))
+        assert r_fx[row] == r_nat[row]
+    assert scaled_err(J_fx, J_nat) <= 1e-15
+    assert scaled_err(r_fx, r_nat) <= 1e-13
+
+
+def test_wide_but_exact_kappa_range():
+    # kappa spanning 2^6 within rows (exact in the fixed point): still within a few ulps of FP64
+    n = (7, 6, 5)
+    kap = np.exp2(np.random.default_rng(7).integers(0, 7, n[0] * n[1] * n[2])).astype(np.float64)
+    kap *= 1.0 + 0.1 * np.random.default_rng(8).random(kap.size)
+    G = gpu_problem(_cfg(kap, n))
+    u = _u(G, 9)
+    _, J_fx = _assemble(G, u, native=False)
+    _, J_nat = _assemble(G, u, native=True)
+    nz = J_nat != 0
+    rel = np.abs(J_fx[nz] - J_nat[nz]) / np.abs(J_nat[nz])
+    assert rel.max() <= 8 * np.finfo(np.float64).eps
+
+
+def test_mixed_j32_bits_unchanged():
+    n = (10, 9, 8)
+    kap = np.exp(np.random.default_rng(10).standard_normal(n[0] * n[1] * n[2]))
+    G = gpu_problem(_cfg(kap, n))
+    u = _u(G, 11)
+    r_fx, J_fx = _assemble(G, u, native=False, fp32=True)
+    r_nat, J_nat = _assemble(G, u, native=True, fp32=True)
+    assert np.array_equal(J_fx, J_nat)
+    assert scaled_err(r_fx, r_nat) <= 1e-13
