@@ -313,7 +313,8 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": WORKLOAD, "cells": cells, "dofs": info.n_dofs, "nnz": info.nnz,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed before every timed step (256 MB write, outside the step's CUDA events)",
-                   "path": "factored row-gather (kappa_c * K_ref, one CSR row per thread, smem-staged 16B stores)"},
+                   "path": "factored row-gather (kappa_c * K_ref, one CSR row per thread, smem-staged 16B stores; "
+                            "kappa sums exact in 64-bit fixed point, rounded once to FP64; FP64 products and residual)"},
         "dof_per_s": world * info.n_dofs * args.steps / (tot64 * 1e-3),
         "mixed": {"value": world * cells * args.steps / (tot32 * 1e-3), "unit": "cells/s",
                   "ms_per_step": tot32 / args.steps, "dtype": "J f32 / residual f64",
