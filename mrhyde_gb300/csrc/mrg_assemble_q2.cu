@@ -497,7 +497,7 @@ void mrg_q2_free(mrg_problem* p) {
   cudaFreeAsync(Q->d_tab32, p->stream);
   cudaFreeAsync(Q->d_err, p->stream);
   if (Q->err_ev) cudaEventDestroy(Q->err_ev);
-  if (Q->h_err) cudaFreeHost(Q->h_err);
+  mrg_pinned_release(Q->h_err);
   if (Q->d_qbuf) cudaFreeAsync(Q->d_qbuf, p->stream);
   mrg_q2tc_free(Q->tc, p->stream);
   delete Q;
@@ -584,7 +584,8 @@ int mrg_launch_q2(mrg_problem* p, const double* u, double* r, void* J, uint32_t 
     if (!Q->tc) {
       int st = mrg_q2tc_create(p, Q->tab_host.data(), Q->T.s, &Q->tc, s);
       if (st) return st;
-      MRG_CUDA(cudaMallocHost(&Q->h_err, sizeof(int)));
+      Q->h_err = (int*)mrg_pinned_slot();
+      if (!Q->h_err) return mrg_fail(MRG_ENOMEM, "pinned error word");
       *Q->h_err = 0;
       MRG_CUDA(cudaEventCreateWithFlags(&Q->err_ev, cudaEventDisableTiming));
     }

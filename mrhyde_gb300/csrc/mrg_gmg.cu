@@ -42,7 +42,7 @@ using namespace mrgdev;
 constexpr int NT = WST;            // threads per CTA
 constexpr int NU = 2;              // Chebyshev degree (pre and post smoothing)
 constexpr double CHEB_LO = 0.25;   // lower end of the smoothed interval, fraction of the bound
-constexpr int GCHUNK = 4;          // CG iterations per captured graph
+constexpr int GCHUNK = 2;          // Krylov iterations per captured graph (2: fewer nodes to instantiate and fewer iterations past convergence than 4; measured on small and large problems)
 constexpr int MAXC = 32;           // largest coarsest level solved densely
 constexpr int MAXLEV = 16;
 constexpr int64_t RAP_WARP_ROWS = 24576;  // Galerkin sweeps with fewer output rows: one warp per row
@@ -945,7 +945,7 @@ void free_hier(Hier<T>* H, cudaStream_t s) {
   for (void* ptr : {(void*)H->cinv, (void*)H->lmax, (void*)H->coef, (void*)H->err, (void*)H->x, (void*)H->r, (void*)H->p,
                     (void*)H->q, (void*)H->parts, (void*)H->S})
     if (ptr) cudaFreeAsync(ptr, s);
-  if (H->h_S) cudaFreeHost(H->h_S);
+  mrg_pinned_release(H->h_S);
   delete H;
 }
 
@@ -1038,7 +1038,9 @@ int build_hier(const mrg_problem* p, Hier<T>*& out, cudaStream_t s) {
       cudaMallocAsync(&H->parts, nparts * sizeof(double), s) != cudaSuccess ||
       cudaMallocAsync(&H->S, sizeof(GScal), s) != cudaSuccess)
     return fail(mrg_fail(MRG_ENOMEM, "multigrid workspace"));
-  if (cudaMallocHost(&H->h_S, sizeof(GScal)) != cudaSuccess) return fail(mrg_fail(MRG_ENOMEM, "multigrid pinned scalars"));
+  static_assert(sizeof(GScal) <= 256, "pinned slot size");
+  H->h_S = (GScal*)mrg_pinned_slot();
+  if (!H->h_S) return fail(mrg_fail(MRG_ENOMEM, "multigrid pinned scalars"));
   MRG_CUDA(cudaMemsetAsync(H->S, 0, sizeof(GScal), s));
   MRG_CUDA(cudaMemsetAsync(H->parts, 0, nparts * sizeof(double), s));
   out = H;

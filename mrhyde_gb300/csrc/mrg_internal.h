@@ -16,6 +16,12 @@ void mrg_set_error(const std::string& msg);
 int mrg_fail(int status, const std::string& msg);
 int mrg_cuda_check(cudaError_t e, const char* what);
 
+// Small pinned host slots (<= 256 bytes: device scalars read back by the host) from a process-wide pool.
+// cudaMallocHost / cudaFreeHost per problem cost driver round trips and can synchronise the device,
+// stalling every other stream in flight; the pool's chunks are pinned once and kept.
+void* mrg_pinned_slot();
+void mrg_pinned_release(void* p);
+
 #define MRG_CUDA(call)                                          \
   do {                                                          \
     cudaError_t e__ = (call);                                   \

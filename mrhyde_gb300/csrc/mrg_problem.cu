@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -21,6 +22,34 @@ int mrg_fail(int status, const std::string& msg) {
 int mrg_cuda_check(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
   return (e == cudaErrorMemoryAllocation) ? MRG_ENOMEM : MRG_ECUDA;
+}
+
+// ------------------------------------------------------------------------------------------------
+// pinned slot pool
+// ------------------------------------------------------------------------------------------------
+namespace {
+constexpr size_t PIN_SLOT = 256, PIN_CHUNK = 64 * 1024;
+std::mutex g_pin_mu;
+std::vector<void*> g_pin_free;
+}  // namespace
+
+void* mrg_pinned_slot() {
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  if (g_pin_free.empty()) {
+    void* chunk = nullptr;
+    if (cudaMallocHost(&chunk, PIN_CHUNK) != cudaSuccess) return nullptr;
+    for (size_t off = 0; off < PIN_CHUNK; off += PIN_SLOT) g_pin_free.push_back((char*)chunk + off);
+  }
+  void* p = g_pin_free.back();
+  g_pin_free.pop_back();
+  std::memset(p, 0, PIN_SLOT);
+  return p;
+}
+
+void mrg_pinned_release(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free.push_back(p);
 }
 
 extern "C" int mrg_last_error(char* buf, size_t len) {

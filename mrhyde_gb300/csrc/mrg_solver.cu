@@ -447,7 +447,7 @@ void mrg_solver_free(mrg_problem* p) {
                     (void*)w->x32, (void*)w->r32, (void*)w->z32, (void*)w->p32, (void*)w->q32, (void*)w->minv32,
                     (void*)w->s, (void*)w->F, (void*)w->du, (void*)w->J64, (void*)w->J32})
     if (ptr) cudaFreeAsync(ptr, s);
-  delete w->h_s;
+  mrg_pinned_release(w->h_s);
   delete w;
   p->work = nullptr;
 }
@@ -471,7 +471,9 @@ static int ensure_work(mrg_problem* p, bool need64, bool need32, cudaStream_t st
   if (!w->s) {
     MRG_CUDA(cudaMallocAsync(&w->s, sizeof(PcgScal), st));
     MRG_CUDA(cudaMemsetAsync(w->s, 0, sizeof(PcgScal), st));
-    w->h_s = new PcgScal();
+    static_assert(sizeof(PcgScal) <= 256, "pinned slot size");
+    w->h_s = (PcgScal*)mrg_pinned_slot();
+    if (!w->h_s) return mrg_fail(MRG_ENOMEM, "solver pinned scalars");
   }
   if (need64 && !w->r) {
     MRG_CUDA(cudaMallocAsync(&w->r, n * sizeof(double), st));
