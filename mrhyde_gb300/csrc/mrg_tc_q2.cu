@@ -351,15 +351,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
-// cells along one axis that contain both node i and node j (p = 2): [lo, hi]
-__device__ __forceinline__ void pair_cells(int i, int j, int nc, int& lo, int& hi) {
-  const int mn = i < j ? i : j, mx = i < j ? j : i;
-  lo = (mx - 1) >> 1;
-  if (lo < 0) lo = 0;
-  hi = mn >> 1;
-  if (hi > nc - 1) hi = nc - 1;
-}
-
 constexpr int GT = 256;   // gather threads per CTA
 constexpr int GRUN = 16;  // consecutive rows a warp takes at a time
 
