@@ -548,6 +548,22 @@ def run_profile(args, local_rank):
 
     torch.cuda.set_device(local_rank)
     mrhyde_gb300.load()
+    if args.profile == "c2newton":  # C2 mixed Newton with multigrid CG (the bench's solve leg): warm-up, then solve(s)
+        from mrhyde_gb300 import Problem, SolverManager
+        from mrhyde_gb300.workloads import c2
+
+        P = Problem(**c2(n=args.n))
+        S = SolverManager(P, nonlinear_tol=1e-10, max_nonlinear_iters=12, linear_tol=1e-4, linear_maxiter=20000,
+                          mixed_precision=True, preconditioner="gmg")
+        for _ in range(args.warmup + args.steps):
+            uu = P.new_vector()
+            t = time.perf_counter()
+            res = S.nonlinearSolver(uu, raise_on_noconv=False)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+        print(json.dumps({"profile": "c2newton", "steps": args.steps, "seconds_last": dt,
+                          "newton_iters": res.outer_iterations, "krylov_iters": res.iterations}))
+        return
     if args.profile == "c3gmg":  # C3 mixed Newton with p-multigrid BiCGStab: warm-up solve(s), then the solve(s)
         from mrhyde_gb300 import Problem, SolverManager
         from mrhyde_gb300.workloads import c3
@@ -628,7 +644,7 @@ def main():
     ap.add_argument("--c3-n", type=int, default=64)
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c3gmg", "c4"],
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
