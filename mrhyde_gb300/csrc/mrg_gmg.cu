@@ -506,6 +506,47 @@ __global__ void __launch_bounds__(NT) k_resid(LevDev<T> L, const T* __restrict__
 }
 
 // b_c = P^T r_f
+// Per-axis transfer slots with validity flags (registers, no run-time indexed arrays): children of a
+// coarse node (fine 2c-1, 2c, 2c+1 on a coarsened axis, the node itself otherwise) and parents of a
+// fine node (1 or 2).  Same sets, order and weights as axis_children / axis_parents.
+__device__ __forceinline__ void child_slots(int c, int nnf, int nnc, int co, bool in_dim, int ci[3], float cw[3],
+                                            bool ok[3]) {
+  if (!in_dim) {
+    ci[0] = ci[1] = ci[2] = 0;
+    cw[0] = cw[1] = cw[2] = 1.0f;
+    ok[0] = ok[2] = false;
+    ok[1] = true;
+    return;
+  }
+  if (!co) {
+    ci[0] = ci[1] = ci[2] = c;
+    cw[0] = cw[1] = cw[2] = 1.0f;
+    ok[0] = ok[2] = false;
+    ok[1] = true;
+    return;
+  }
+  children3(c, nnf, nnc, ci, cw, ok);
+}
+
+__device__ __forceinline__ void parent_slots(int i, int nnf, int nnc, int co, bool in_dim, int pc[2], float pw[2],
+                                             bool ok[2]) {
+  if (!in_dim) {
+    pc[0] = pc[1] = 0;
+    pw[0] = pw[1] = 1.0f;
+    ok[0] = true;
+    ok[1] = false;
+    return;
+  }
+  const int np = axis_parents(i, nnf, nnc, co, pc, pw);
+  ok[0] = true;
+  ok[1] = np == 2;
+  if (np < 2) {
+    pc[1] = pc[0];
+    pw[1] = 0.0f;
+  }
+}
+
+// b_c = P^T r_f
 template <typename T>
 __global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const T* __restrict__ rf, T* __restrict__ bc,
                                                  const GScal* __restrict__ S) {
@@ -515,20 +556,23 @@ __global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const
     int I[3];
     decompose(gc, n, I[0], I[1], I[2]);
     if (node_fixed(gc, I[0], I[1], I[2])) { bc[n] = T(0); continue; }
-    int ci[3][3];
-    float cw[3][3];
-    int nci[3];
-    for (int k = 0; k < 3; ++k) {
-      if (k < gf.dim) nci[k] = axis_children(I[k], gf.nn[k], gc.nn[k], X.co[k], ci[k], cw[k]);
-      else { nci[k] = 1; ci[k][0] = 0; cw[k][0] = 1.0f; }
-    }
+    int c0[3], c1[3], c2[3];
+    float w0[3], w1[3], w2[3];
+    bool k0[3], k1[3], k2[3];
+    child_slots(I[0], gf.nn[0], gc.nn[0], X.co[0], gf.dim > 0, c0, w0, k0);
+    child_slots(I[1], gf.nn[1], gc.nn[1], X.co[1], gf.dim > 1, c1, w1, k1);
+    child_slots(I[2], gf.nn[2], gc.nn[2], X.co[2], gf.dim > 2, c2, w2, k2);
     T s = T(0);
-    for (int a2 = 0; a2 < nci[2]; ++a2)
-      for (int a1 = 0; a1 < nci[1]; ++a1)
-        for (int a0 = 0; a0 < nci[0]; ++a0) {
-          const int ix = ci[0][a0], iy = ci[1][a1], iz = ci[2][a2];
+#pragma unroll
+    for (int a2 = 0; a2 < 3; ++a2)
+#pragma unroll
+      for (int a1 = 0; a1 < 3; ++a1)
+#pragma unroll
+        for (int a0 = 0; a0 < 3; ++a0) {
+          if (!(k2[a2] && k1[a1] && k0[a0])) continue;
+          const int ix = c0[a0], iy = c1[a1], iz = c2[a2];
           if (node_fixed(gf, ix, iy, iz)) continue;
-          s += (T)(cw[0][a0] * cw[1][a1] * cw[2][a2]) * rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)];
+          s += (T)(w0[a0] * w1[a1] * w2[a2]) * rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)];
         }
     bc[n] = s;
   }
@@ -544,20 +588,22 @@ __global__ void __launch_bounds__(NT) k_prolong(Grid gf, Grid gc, Xfer X, const 
     int i[3];
     decompose(gf, n, i[0], i[1], i[2]);
     if (node_fixed(gf, i[0], i[1], i[2])) continue;
-    int pc[3][2];
-    float pw[3][2];
-    int np[3];
-    for (int k = 0; k < 3; ++k) {
-      if (k < gf.dim) np[k] = axis_parents(i[k], gf.nn[k], gc.nn[k], X.co[k], pc[k], pw[k]);
-      else { np[k] = 1; pc[k][0] = 0; pw[k][0] = 1.0f; }
-    }
+    int p0[2], p1[2], p2[2];
+    float w0[2], w1[2], w2[2];
+    bool k0[2], k1[2], k2[2];
+    parent_slots(i[0], gf.nn[0], gc.nn[0], X.co[0], gf.dim > 0, p0, w0, k0);
+    parent_slots(i[1], gf.nn[1], gc.nn[1], X.co[1], gf.dim > 1, p1, w1, k1);
+    parent_slots(i[2], gf.nn[2], gc.nn[2], X.co[2], gf.dim > 2, p2, w2, k2);
     T s = T(0);
-    for (int b2 = 0; b2 < np[2]; ++b2)
-      for (int b1 = 0; b1 < np[1]; ++b1)
-        for (int b0 = 0; b0 < np[0]; ++b0) {
-          if (node_fixed(gc, pc[0][b0], pc[1][b1], pc[2][b2])) continue;
-          s += (T)(pw[0][b0] * pw[1][b1] * pw[2][b2]) *
-               xc[pc[0][b0] + (int64_t)gc.nn[0] * (pc[1][b1] + (int64_t)gc.nn[1] * pc[2][b2])];
+#pragma unroll
+    for (int b2 = 0; b2 < 2; ++b2)
+#pragma unroll
+      for (int b1 = 0; b1 < 2; ++b1)
+#pragma unroll
+        for (int b0 = 0; b0 < 2; ++b0) {
+          if (!(k2[b2] && k1[b1] && k0[b0])) continue;
+          if (node_fixed(gc, p0[b0], p1[b1], p2[b2])) continue;
+          s += (T)(w0[b0] * w1[b1] * w2[b2]) * xc[p0[b0] + (int64_t)gc.nn[0] * (p1[b1] + (int64_t)gc.nn[1] * p2[b2])];
         }
     xf[n] += s;
   }
