@@ -502,6 +502,7 @@ def serve_replicated(reqs, slots, realtime, rank=0, world=1, dist=None):
     from mrhyde_gb300 import serving
 
     srv = serving.Server(hbm_budget_bytes=80 * 10**9, slots=slots)
+    srv.warmup()
     mine = serving.shard(reqs, rank, world) if world > 1 else reqs
     summ = srv.run(mine, realtime=realtime)
     summ["peak_active"] = srv.peak_active

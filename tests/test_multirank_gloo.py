@@ -31,6 +31,11 @@ class _FakeSolve:
         return R(), None, float(req.rid), 10 * req.n
 
 
+class _FakeStream:  # the fake solve needs no stream; the server's warm-up synchronises it
+    def synchronize(self):
+        pass
+
+
 def _worker(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
@@ -40,7 +45,7 @@ def _worker(rank, world, port, q):
 
         out = {"max": bench.max_over_ranks(1.5 + rank, dist, "cpu")}
         serving.solve_request = _FakeSolve()
-        torch.cuda.Stream = lambda: None  # the fake needs no stream
+        torch.cuda.Stream = _FakeStream
         reqs = serving.poisson_stream(rate=2000.0, count=24, edge=(4, 6), seed=3)
         mine = serving.shard(reqs, rank, world)
         ids = [None] * world

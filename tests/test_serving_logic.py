@@ -108,3 +108,23 @@ def test_unexpected_exception_fails_only_that_request(monkeypatch):
     out = srv.run(reqs, realtime=False)
     assert out["requests"] == 6 and out["ok"] == 5
     assert [rid for rid, _ in srv.errors] == [2]
+
+
+def test_warmup_solves_each_kind_and_precision(monkeypatch):
+    seen = []
+
+    class Rec(FakeSolve):
+        def __call__(self, req, stream, keep, preconditioner="gmg"):
+            seen.append((req.kind, req.mixed, req.n, keep, preconditioner))
+            return super().__call__(req, stream, keep, preconditioner)
+
+    class Stream:
+        def synchronize(self):
+            seen.append("sync")
+
+    monkeypatch.setattr(serving, "solve_request", Rec())
+    monkeypatch.setattr(serving.torch.cuda, "Stream", Stream)
+    srv = serving.Server(slots=2, preconditioner="jacobi")
+    srv.warmup()
+    assert sorted(seen[:-1]) == sorted((k, m, 64, False, "jacobi") for k in ("thermal", "nonlinear") for m in (True, False))
+    assert seen[-1] == "sync" and srv.results == []
