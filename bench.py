@@ -295,9 +295,7 @@ def run_ours(args, rank, world, local_rank):
     algo32 = algorithmic_bytes(cells, info.n_dofs, info.nnz, 4)
     ach64 = algo64 / (ms_step * 1e-3) / 1e9
     traffic = read_profile_traffic("k_fact_hex_fp64_c2_128")
-    # FP64 instructions per launch: 27 DMUL (K(off) * S(off)) + 27 DFMA (residual) per free row; the kappa
-    # sums are exact fixed-point sums on the integer pipes (19 DADD more per row with MRG_ASM_NATIVE_FP64)
-    dp_ops = 54 * (info.n_dofs - info.n_fixed)
+    dp_ops = fp64_instructions(cfg)
     import ctypes
 
     from mrhyde_gb300 import _lib as LL
@@ -314,7 +312,8 @@ def run_ours(args, rank, world, local_rank):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed before every timed step (256 MB write, outside the step's CUDA events)",
                    "path": "factored row-gather (kappa_c * K_ref, one CSR row per thread, smem-staged 16B stores; "
-                            "kappa sums exact in 64-bit fixed point, rounded once to FP64; FP64 products and residual)"},
+                            "kappa sums exact in 64-bit fixed point, rounded once to FP64; FP64 products and residual; "
+                            "the axis-neighbour entries of cubic cells (coefficient +0) without FP64 instructions)"},
         "dof_per_s": world * info.n_dofs * args.steps / (tot64 * 1e-3),
         "mixed": {"value": world * cells * args.steps / (tot32 * 1e-3), "unit": "cells/s",
                   "ms_per_step": tot32 / args.steps, "dtype": "J f32 / residual f64",
@@ -495,6 +494,23 @@ def max_over_ranks(x: float, dist=None, device="cpu") -> float:
     t = torch.tensor([float(x)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def fp64_instructions(cfg):
+    """FP64 instructions of one FP64 Jac+res launch of the factored Q1 kernel on a box with Dirichlet rows on
+    the x = 0 and x = 1 faces: a DMUL (K(off) * S(off)) and a DFMA (residual) per entry of a free row, except
+    the axis-neighbour entries of cubic cells, whose coefficient is +0 and which take no FP64 instruction.
+    The kappa sums are exact fixed-point sums on the integer pipes (no FP64 instruction)."""
+    import numpy as np
+
+    n = [c + 1 for c in cfg["n"]]
+    h = [(b - a) / c for a, b, c in zip(cfg["lo"], cfg["hi"], cfg["n"])]
+    nb = [(np.arange(m) > 0).astype(np.int64) + (np.arange(m) < m - 1) for m in n]  # neighbours per axis
+    bx, by, bz = nb[0][1:-1][None, None, :], nb[1][None, :, None], nb[2][:, None, None]  # free rows: 0 < ix < nx
+    entries = int(((1 + bx) * (1 + by) * (1 + bz)).sum())
+    if h[0] == h[1] == h[2]:
+        entries -= int((bx + by + bz).sum())
+    return 2 * entries
 
 
 def serve_replicated(reqs, slots, realtime, rank=0, world=1, dist=None):

@@ -130,10 +130,12 @@ enum {
   MRG_ASM_TENSOR_CORES = 4096u,/* Q2 FP32 Jacobian: element contractions on tcgen05 tensor cores (3xTF32);
                                   the default for Q2 FP32 Jacobians, kept for explicitness */
   MRG_ASM_CUDA_CORES = 8192u,  /* Q2 FP32 Jacobian: force the CUDA-core contraction instead */
-  MRG_ASM_NATIVE_FP64 = 16384u /* Q1 factored path: form the kappa sums S(off) with FP64 additions.  By
-                                  default each S(off) is the exact sum (64-bit fixed point on the integer
-                                  pipes) rounded once to FP64, for every row whose kappa lie within 2^7 of each
-                                  other; products and residual FMAs are FP64 either way */
+  MRG_ASM_NATIVE_FP64 = 16384u /* Q1 factored path: every kappa sum, product and residual FMA as an FP64
+                                  instruction.  By default each S(off) is the exact sum (64-bit fixed point
+                                  on the integer pipes) rounded once to FP64, for every row whose kappa lie
+                                  within 2^7 of each other, and on cubic cells the axis-neighbour entries,
+                                  whose coefficient is +0, are formed without FP64 instructions (the same
+                                  bits: +0 * S) */
 };
 
 /* ---- problem lifetime ------------------------------------------------------------------------- */

@@ -53,6 +53,10 @@ __device__ __forceinline__ void neumaier_add(float& sum, float& comp, float v) {
   sum = t;
 }
 
+__device__ __forceinline__ bool nonfinite(double v) {
+  return ((unsigned)__double2hiint(v) & 0x7ff00000u) == 0x7ff00000u;
+}
+
 __device__ __forceinline__ int64_t row_ptr_of(const Grid& g, int64_t n, int64_t nrows) {
   if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
   int ix, iy, iz;
@@ -106,6 +110,7 @@ struct FactArgs {
   const double* B[3];
   int64_t nrows, nnz;
   int fixed;          // 1: exact fixed-point kappa sums (mrg_fixmul.cuh) where a row's kappa allow; 0: FP64 additions
+  int zax;            // 1: K of the three axis classes (1, 2, 4) is +0 (cubic cells)
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -113,7 +118,7 @@ struct FactArgs {
 // ------------------------------------------------------------------------------------------------
 // Occupancy floors chosen by measurement: FP64 Jacobians 6 CTAs per SM (80 registers, no spills; 0.266 ->
 // 0.253 ms on C2), FP32 Jacobians 5 (96 registers; 0.252 -> 0.232 ms against the compiler's 117)
-template <typename JT, bool DOJ, bool DOR, bool OVW>
+template <typename JT, bool DOJ, bool DOR, bool OVW, bool ZAX>
 __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const FactArgs A, const double* __restrict__ u,
                                                   const double* __restrict__ kap, const float* __restrict__ kap32,
                                                   double* __restrict__ r, JT* __restrict__ J) {
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
               emax = max(emax, e & 0x7ff);
             }
           }
-      fx = fx && emax >= 60;  // rounded sums are normal numbers
+      fx = fx && emax >= 60 && emax <= 2042;  // rounded sums are normal, finite numbers
       // S[dz][dy][dx] = sum of kappa over the cells shared by node and node+off
       double S[3][3][3];
       if (fx) {
@@ -312,6 +317,7 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
       int dpos = 0;
       int pos = 0;
       const int64_t plane = (int64_t)NX * NY;
+      bool ubad = false;  // ZAX: a skipped residual term is NaN
 #pragma unroll
       for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
@@ -322,9 +328,20 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
               const int cls = (dx != 0) + 2 * (dy != 0) + 4 * (dz != 0);
               const double s = S[dz + 1][dy + 1][dx + 1];
               if (!MIXED) {
-                const double a = A.Kp[cls] * s;
-                if (DOJ) sv[loc + pos] = (JT)a;
-                if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+                if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
+                  // K = +0: the product +0 * s is a zero with the sign of s (NaN for a non-finite s), and
+                  // the residual term -(+-0) * u leaves acc unchanged unless s or u is not finite (then
+                  // NaN).  No FP64 instruction: on cubic cells 12 of an interior row's 54.
+                  const bool sbad = nonfinite(s);
+                  if (DOJ)
+                    sv[loc + pos] = (JT)__longlong_as_double(
+                        sbad ? 0x7fffffffffffffffll : (long long)((unsigned long long)__double_as_longlong(s) & 0x8000000000000000ull));
+                  if (DOR) ubad |= sbad | nonfinite(__ldg(u + n + dx + (int64_t)NX * dy + plane * dz));
+                } else {
+                  const double a = A.Kp[cls] * s;
+                  if (DOJ) sv[loc + pos] = (JT)a;
+                  if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+                }
               } else {
                 if (DOJ) {
                   if (cls == 0) {
@@ -345,6 +362,7 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
 #pragma unroll
           for (int c = 0; c < 8; ++c) acc = fma(-A.Kp[c], t[c], acc);
         }
+        if (ZAX && ubad) acc = __longlong_as_double(0x7fffffffffffffffll);
         if (OVW) r[n] = acc; else r[n] += acc;
       }
     }
@@ -756,7 +774,9 @@ cudaError_t launch_fact(const mrg_problem* p, const FactArgs& A, const double* u
   const int smem = DOJ ? (FT * (p->g.dim == 3 ? 27 : 9) + 16 / (int)sizeof(JT)) * (int)sizeof(JT) : 0;
   const unsigned grid = nblk(p->ndof, FT);
   if (p->g.dim == 3) {
-    auto kern = k_fact_hex<JT, DOJ, DOR, OVW>;
+    auto kern = k_fact_hex<JT, DOJ, DOR, OVW, false>;
+    if constexpr (sizeof(JT) == 8)
+      if (A.zax) kern = k_fact_hex<JT, DOJ, DOR, OVW, true>;  // FP64 only
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
   } else {
@@ -831,6 +851,8 @@ int mrg_launch_factored(mrg_problem* p, const double* u, double* r, void* J, uin
   A.load = p->source_amp * p->cell_load;
   for (int k = 0; k < 4; ++k) A.loadk[k] = std::ldexp(A.load, k);  // exact: a power-of-two scaling
   A.fixed = (flags & MRG_ASM_NATIVE_FP64) ? 0 : 1;
+  auto pos0 = [&](int c) { return p->Kp[c] == 0.0 && !std::signbit(p->Kp[c]); };
+  A.zax = (A.fixed && p->g.dim == 3 && pos0(1) && pos0(2) && pos0(4)) ? 1 : 0;  // native: every product a DMUL
   if (A.src_sin) {
     A.B[0] = p->d_srcB;
     A.B[1] = p->d_srcB + p->g.nn[0];

@@ -1,5 +1,6 @@
 // Problem lifetime, structure queries, coefficients, Dirichlet data and the assembly dispatcher
 // of the C ABI declared in include/mrhyde_gb300.h.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -419,6 +420,13 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
       }
       P->Kp[j] = s;
     }
+    // Classes whose coefficient cancels in exact arithmetic (the axis neighbours of cubic cells:
+    // -h/9 + h/18 + h/18) come out of the quadrature as rounding residue, ~1e-17 of the largest; a
+    // coefficient within 64 ulps of the largest is that residue and is set to the exact zero.
+    double kmax = 0.0;
+    for (int j = 0; j < nvpe; ++j) kmax = std::max(kmax, std::fabs(P->Kp[j]));
+    for (int j = 0; j < nvpe; ++j)
+      if (std::fabs(P->Kp[j]) <= 64.0 * 2.220446049250313e-16 * kmax) P->Kp[j] = 0.0;
     double ld = 0.0;
     for (int q = 0; q < nq; ++q) ld += tphi[0 * nq + q] * tw[q] * detJ;
     P->cell_load = ld;

@@ -148,3 +148,63 @@ def test_mixed_j32_bits_unchanged():
     r_nat, J_nat = _assemble(G, u, native=True, fp32=True)
     assert np.array_equal(J_fx, J_nat)
     assert scaled_err(r_fx, r_nat) <= 1e-13
+
+
+# ---- cubic cells: the axis-neighbour coefficient is +0 and those entries take no FP64 instruction --------
+def _axis_slots(G, n):
+    """CSR slots of the axis-neighbour entries (column differs from the row in exactly one coordinate)."""
+    rp, ci = G.graph()
+    rp, ci = rp.cpu().numpy(), ci.cpu().numpy()
+    nx, ny = n[0] + 1, n[1] + 1
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    d = [np.abs(rows % nx - ci % nx), np.abs(rows // nx % ny - ci // nx % ny), np.abs(rows // (nx * ny) - ci // (nx * ny))]
+    return ((d[0] != 0).astype(int) + (d[1] != 0) + (d[2] != 0)) == 1
+
+
+@pytest.mark.parametrize("kind", ["integer", "lognormal"])
+def test_cube_axis_entries(kind):
+    n = (8, 8, 8)
+    rng = np.random.default_rng(12)
+    kap = rng.integers(1, 9, 512).astype(np.float64) if kind == "integer" else np.exp(rng.standard_normal(512))
+    cfg = _cfg(kap, n, hi=(0.5, 0.5, 0.5))
+    G = gpu_problem(cfg)
+    u = _u(G, 13)
+    r_fx, J_fx = _assemble(G, u, native=False)
+    r_nat, J_nat = _assemble(G, u, native=True)   # every product a DMUL
+    ax = _axis_slots(G, n)
+    assert ax.sum() > 0 and np.all(J_fx[ax].view(np.uint64) == 0)  # +0
+    assert np.array_equal(J_fx[ax].view(np.uint64), J_nat[ax].view(np.uint64))
+    if kind == "integer":
+        assert np.array_equal(J_fx.view(np.uint64), J_nat.view(np.uint64))
+        assert np.array_equal(r_fx, r_nat)
+    else:
+        assert scaled_err(J_fx, J_nat) <= 1e-15
+        assert scaled_err(r_fx, r_nat) <= 1e-13
+    r_o, J_o = oracle_problem(cfg).assemble(u)
+    assert scaled_err(J_fx, J_o) <= TOL64
+    assert scaled_err(r_fx, r_o) <= TOL64
+    r_r, _ = _assemble(G, u, native=False, jac=False)
+    assert np.array_equal(r_r, r_fx)
+
+
+def test_cube_signed_and_nonfinite_entries():
+    # negative kappa (zero entries with the sign of S), kappa near the top of the range (sums overflow to
+    # inf: +0 * inf is NaN) and a non-finite u: the same values as the plain FP64 instructions
+    n = (6, 6, 6)
+    kap = np.random.default_rng(14).integers(1, 9, 216).astype(np.float64)  # exact sums on both paths
+    kap[17] = -12.5
+    kap[100] = 1.5e308
+    kap[101] = 1.2e308
+    cfg = _cfg(kap, n)
+    G = gpu_problem(cfg)
+    u = _u(G, 15)
+    u[150] = np.inf
+    u[40] = np.nan
+    r_fx, J_fx = _assemble(G, u, native=False)
+    r_nat, J_nat = _assemble(G, u, native=True)
+    fin = ~np.isnan(J_nat)
+    assert np.array_equal(np.isnan(J_fx), ~fin)
+    assert np.array_equal(J_fx[fin].view(np.uint64), J_nat[fin].view(np.uint64))
+    assert np.array_equal(r_fx, r_nat, equal_nan=True)
+    ax = _axis_slots(G, n)
+    assert (np.signbit(J_fx[ax & fin])).any() and (~np.signbit(J_fx[ax & fin])).any()
