@@ -134,8 +134,8 @@ enum {
                                   instruction.  By default each S(off) is the exact sum (64-bit fixed point
                                   on the integer pipes) rounded once to FP64, for every row whose kappa lie
                                   within 2^7 of each other, and on cubic cells the axis-neighbour entries,
-                                  whose coefficient is +0, are formed without FP64 instructions (the same
-                                  bits: +0 * S) */
+                                  whose coefficient is +0, and their residual terms take no FP64
+                                  instruction (the same values: +0 * S, NaN from a non-finite S or u) */
 };
 
 /* ---- problem lifetime ------------------------------------------------------------------------- */

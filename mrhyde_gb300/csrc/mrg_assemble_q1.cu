@@ -237,6 +237,10 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
             for (int x = 0; x < 3; ++x) {
               if (z != 1 && y != 1 && x != 1) {
                 S[z][y][x] = __longlong_as_double((long long)kb[z >> 1][y >> 1][x >> 1]);
+              } else if (ZAX && (z != 1) + (y != 1) + (x != 1) == 1) {
+                // axis entry, K = +0: every kappa of the row is >= 0 and finite, so the entry is +0 for
+                // any S >= 0 and the sum is not rounded
+                S[z][y][x] = 0.0;
               } else {
                 const uint64_t q = (z == 0) ? qxy[0][y][x] : (z == 2 ? qxy[1][y][x] : qxy[0][y][x] + qxy[1][y][x]);
                 S[z][y][x] = __longlong_as_double((long long)mrgfix::fix_to_f64_bits(q, emax));
@@ -317,7 +321,7 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
       int dpos = 0;
       int pos = 0;
       const int64_t plane = (int64_t)NX * NY;
-      bool ubad = false;  // ZAX: a skipped residual term is NaN
+      bool ubad = false;  // ZAX: a skipped residual term is NaN (FP64 and mixed)
 #pragma unroll
       for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
@@ -352,7 +356,12 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
                     neumaier_add(osum, ocomp, v);
                   }
                 }
-                if (DOR) t[cls] = fma(s, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), t[cls]);
+                if (DOR) {
+                  const double uv = __ldg(u + n + dx + (int64_t)NX * dy + plane * dz);
+                  // K = +0 class: K * t is +0 unless S or u is not finite (the same rule as FP64 above)
+                  if (ZAX && (cls == 1 || cls == 2 || cls == 4)) ubad |= nonfinite(s) | nonfinite(uv);
+                  else t[cls] = fma(s, uv, t[cls]);
+                }
               }
               ++pos;
             }
@@ -360,7 +369,8 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
       if (DOR) {
         if (MIXED) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c) acc = fma(-A.Kp[c], t[c], acc);
+          for (int c = 0; c < 8; ++c)
+            if (!(ZAX && (c == 1 || c == 2 || c == 4))) acc = fma(-A.Kp[c], t[c], acc);
         }
         if (ZAX && ubad) acc = __longlong_as_double(0x7fffffffffffffffll);
         if (OVW) r[n] = acc; else r[n] += acc;
@@ -774,9 +784,7 @@ cudaError_t launch_fact(const mrg_problem* p, const FactArgs& A, const double* u
   const int smem = DOJ ? (FT * (p->g.dim == 3 ? 27 : 9) + 16 / (int)sizeof(JT)) * (int)sizeof(JT) : 0;
   const unsigned grid = nblk(p->ndof, FT);
   if (p->g.dim == 3) {
-    auto kern = k_fact_hex<JT, DOJ, DOR, OVW, false>;
-    if constexpr (sizeof(JT) == 8)
-      if (A.zax) kern = k_fact_hex<JT, DOJ, DOR, OVW, true>;  // FP64 only
+    auto kern = A.zax ? k_fact_hex<JT, DOJ, DOR, OVW, true> : k_fact_hex<JT, DOJ, DOR, OVW, false>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
   } else {

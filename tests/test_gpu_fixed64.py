@@ -208,3 +208,21 @@ def test_cube_signed_and_nonfinite_entries():
     assert np.array_equal(r_fx, r_nat, equal_nan=True)
     ax = _axis_slots(G, n)
     assert (np.signbit(J_fx[ax & fin])).any() and (~np.signbit(J_fx[ax & fin])).any()
+
+
+def test_cube_mixed_j32_unchanged_and_residual():
+    n = (8, 8, 8)
+    kap = np.exp(np.random.default_rng(16).standard_normal(512))
+    cfg = _cfg(kap, n, hi=(0.5, 0.5, 0.5))
+    G = gpu_problem(cfg)
+    u = _u(G, 17)
+    r_fx, J_fx = _assemble(G, u, native=False, fp32=True)
+    r_nat, J_nat = _assemble(G, u, native=True, fp32=True)
+    assert np.array_equal(J_fx.view(np.uint32), J_nat.view(np.uint32))
+    assert scaled_err(r_fx, r_nat) <= 1e-13
+    r64, _ = _assemble(G, u, native=False)
+    assert scaled_err(r_fx, r64) <= 1e-13
+    u[77] = np.nan
+    r_fx, _ = _assemble(G, u, native=False, fp32=True)
+    r_nat, _ = _assemble(G, u, native=True, fp32=True)
+    assert np.array_equal(np.isnan(r_fx), np.isnan(r_nat)) and np.isnan(r_fx).sum() > 1
