@@ -124,30 +124,41 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
                                                   double* __restrict__ r, JT* __restrict__ J) {
   constexpr bool MIXED = sizeof(JT) == 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int64_t s_seg[2];
   const Grid& g = A.g;
   const int64_t n0 = (int64_t)blockIdx.x * FT;
   const int64_t n = n0 + threadIdx.x;
   const int64_t nend = (n0 + FT < A.nrows) ? n0 + FT : A.nrows;
-  const int64_t seg0 = row_ptr_of(g, n0, A.nrows);
-  const int64_t seg1 = row_ptr_of(g, nend, A.nrows);
+  const bool active = n < A.nrows;
+  const int NX = g.nn[0], NY = g.nn[1], NZ = g.nn[2];
+  int ix = 0, iy = 0, iz = 0, cx = 1, cy = 1, cz = 1;
+  int64_t myrow = 0;
+  if (active) {
+    decompose(g, n, ix, iy, iz);
+    int lo;
+    axis_range(ix, NX, 1, lo, cx);
+    axis_range(iy, NY, 1, lo, cy);
+    axis_range(iz, NZ, 1, lo, cz);
+    myrow = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+  }
+  // the CTA's CSR segment: from its first row's start to its last row's end (rows are contiguous in CSR)
+  int64_t seg0 = 0, seg1 = 0;
+  if constexpr (DOJ) {
+    if (threadIdx.x == 0) s_seg[0] = myrow;
+    if (n == nend - 1) s_seg[1] = myrow + cx * cy * cz;
+    __syncthreads();
+    seg0 = s_seg[0];
+    seg1 = s_seg[1];
+  }
   // stage so that smem and global share the 16-byte phase
   constexpr int V = 16 / sizeof(JT);
   const int phase = DOJ ? (int)(((uintptr_t)(J + seg0) & 15) / sizeof(JT)) : 0;
   JT* sv = reinterpret_cast<JT*>(smem_raw) + phase;
 
-  bool active = n < A.nrows;
   bool fixed = false;
-  int64_t myrow = 0, diagpos = 0;
+  int64_t diagpos = 0;
   if (active) {
-    int ix, iy, iz;
-    decompose(g, n, ix, iy, iz);
-    const int NX = g.nn[0], NY = g.nn[1], NZ = g.nn[2];
     const int nx = g.nc[0], ny = g.nc[1], nz = g.nc[2];
-    int lo, cx, cy, cz;
-    axis_range(ix, NX, 1, lo, cx);
-    axis_range(iy, NY, 1, lo, cy);
-    axis_range(iz, NZ, 1, lo, cz);
-    myrow = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
     const int64_t loc = myrow - seg0;
     fixed = node_fixed(g, ix, iy, iz);
     const bool vx[3] = {ix > 0, true, ix < NX - 1};
