@@ -29,8 +29,9 @@
 // every role leaves its loop, waits (bounded) for its own copies and MMAs in flight, TMEM is freed and the
 // status word is set, so the host reports MRG_ETIMEOUT instead of hanging.
 //
-// k_q2_gather: one warp per CSR row, one lane per entry: J(i,j) = sum over the cells that contain both
-// nodes (fixed order cz, cy, cx) of E_c[l_i][l_j].  Every element-matrix value is read exactly once and
+// k_q2_gather: one warp per CSR row, one lane per local column, 32 consecutive rows per warp with the row
+// set-up computed lane-parallel: J(i,j) = sum over the cells that contain both nodes (fixed order cz, cy,
+// cx) of E_c[l_i][l_j].  Every element-matrix value is read exactly once and
 // every Jacobian value is written exactly once, coalesced; no atomics, so the result is deterministic.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 constexpr int GT = 256;   // gather threads per CTA
-constexpr int GRUN = 16;  // consecutive rows a warp takes at a time
+constexpr int GRUN = 32;  // consecutive rows a warp takes at a time (one row set-up per lane)
 
 // Row-gather of one CSR row from its NX x NY x NZ boundary-cell block (NX, NY, NZ in {1, 2}).  Lane l < 27
 // stands for local column node l of a cell: for each of the row's cells (fixed order cz, cy, cx) it loads
@@ -379,8 +380,11 @@ __device__ __forceinline__ void gather_cells(float* __restrict__ rb, const float
   }
 }
 
-// One warp per CSR row, GRUN consecutive rows at a time (coordinates and row pointers advance
-// incrementally along the run; a new run starts from a full decomposition).
+// One warp per CSR row, 32 consecutive rows at a time.  The row set-up (coordinates, row pointer, the
+// row's cell block) is computed by lane k for row r0 + k, all 32 at once, and handed to the warp row by
+// row with four shuffles: set-up that every lane used to repeat for every row was most of the kernel's
+// instructions.  A Q2 row's column range along an axis starts at the lowest node of its first cell, so a
+// lane's column position in the row depends only on the row's extents (cx, cy).
 __global__ void __launch_bounds__(GT) k_q2_gather(Grid g, int64_t nrows, const float* __restrict__ E,
                                                   float* __restrict__ J, int ovw) {
   __shared__ float rows[GT / 32][128];
@@ -393,51 +397,63 @@ __global__ void __launch_bounds__(GT) k_q2_gather(Grid g, int64_t nrows, const f
   const bool col = lane < 27;
   const int ljx = lane % 3, ljy = (lane / 3) % 3, ljz = lane / 9;
   for (int64_t r0 = wid * GRUN; r0 < nrows; r0 += nw * GRUN) {
-    int ix, iy, iz;
-    mrgdev::decompose(g, r0, ix, iy, iz);
-    const int64_t r1 = (r0 + GRUN < nrows) ? r0 + GRUN : nrows;
-    for (int64_t n = r0; n < r1; ++n) {
+    // ---- this lane's row r0 + lane: packed set-up
+    // word: cx | cy << 3 | cz << 6 | cell pattern << 9 | fixed << 12 | (local row, or diagonal position) << 13
+    uint32_t word = 0, cell = 0;
+    int64_t rp = 0;
+    if (r0 + lane < nrows) {
+      int ix, iy, iz;
+      mrgdev::decompose(g, r0 + lane, ix, iy, iz);
       const mrgdev::RowInfo R = mrgdev::row_info<2>(g, ix, iy, iz);
-      const int len = R.cx * R.cy * R.cz;
-      float* row = J + R.rp;
+      rp = R.rp;
+      word = (uint32_t)R.cx | ((uint32_t)R.cy << 3) | ((uint32_t)R.cz << 6);
       if (node_fixed(g, ix, iy, iz)) {
-        const int dg = (int)(mrgdev::diag_pos(R, ix, iy, iz) - R.rp);
-        if (ovw) {
-          for (int e = lane; e < len; e += 32) __stcs(row + e, e == dg ? 1.0f : 0.0f);
-        } else if (lane == 0) {
-          row[dg] = 1.0f;
-        }
+        word |= (1u << 12) | ((uint32_t)(mrgdev::diag_pos(R, ix, iy, iz) - R.rp) << 13);
       } else {
         int fx, fy, fz, nxc, nyc, nzc;
         axis_cells(ix, g.nn[0], 2, fx, nxc);
         axis_cells(iy, g.nn[1], 2, fy, nyc);
         axis_cells(iz, g.nn[2], 2, fz, nzc);
-        // cell (fx+kx, fy+ky, fz+kz): local row index li0 - 2 (kx + 3 ky + 9 kz), position of this lane's
-        // column in the row pos0 + 2 (kz cy cx + ky cx + kx)
         const int li0 = (ix - 2 * fx) + 3 * (iy - 2 * fy) + 9 * (iz - 2 * fz);
-        const int pos0 = ((2 * fz + ljz - R.lz) * R.cy + (2 * fy + ljy - R.ly)) * R.cx + (2 * fx + ljx - R.lx);
-        const float* e0 = E + (fx + (int64_t)ncx * (fy + (int64_t)ncy * fz)) * NE + lane;
+        word |= ((uint32_t)((nxc - 1) | ((nyc - 1) << 1) | ((nzc - 1) << 2)) << 9) | ((uint32_t)li0 << 13);
+        cell = (uint32_t)(fx + ncx * (fy + ncy * fz));
+      }
+    }
+    const int nrun = (int)((nrows - r0 < GRUN) ? nrows - r0 : GRUN);
+    for (int k = 0; k < nrun; ++k) {
+      const uint32_t w = __shfl_sync(0xffffffffu, word, k);
+      const uint32_t rlo = __shfl_sync(0xffffffffu, (uint32_t)rp, k);
+      const uint32_t rhi = __shfl_sync(0xffffffffu, (uint32_t)((uint64_t)rp >> 32), k);
+      const uint32_t c = __shfl_sync(0xffffffffu, cell, k);
+      const int cx = (int)(w & 7u), cy = (int)((w >> 3) & 7u), cz = (int)((w >> 6) & 7u);
+      const int len = cx * cy * cz;
+      const int idx = (int)(w >> 13);
+      float* row = J + (int64_t)(((uint64_t)rhi << 32) | rlo);
+      if (w & (1u << 12)) {
+        if (ovw) {
+          for (int e = lane; e < len; e += 32) __stcs(row + e, e == idx ? 1.0f : 0.0f);
+        } else if (lane == 0) {
+          row[idx] = 1.0f;
+        }
+      } else {
+        const int pos0 = (ljz * cy + ljy) * cx + ljx;
+        const float* e0 = E + (int64_t)c * NE + lane;
         for (int e = lane; e < len; e += 32) rb[e] = 0.0f;
         __syncwarp();
-        switch ((nxc - 1) | ((nyc - 1) << 1) | ((nzc - 1) << 2)) {
-          case 0: gather_cells<1, 1, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          case 1: gather_cells<2, 1, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          case 2: gather_cells<1, 2, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          case 3: gather_cells<2, 2, 1>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          case 4: gather_cells<1, 1, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          case 5: gather_cells<2, 1, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          case 6: gather_cells<1, 2, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
-          default: gather_cells<2, 2, 2>(rb, e0, sy, sz, li0, pos0, R.cy, R.cx, col, lane); break;
+        switch ((w >> 9) & 7u) {
+          case 0: gather_cells<1, 1, 1>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          case 1: gather_cells<2, 1, 1>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          case 2: gather_cells<1, 2, 1>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          case 3: gather_cells<2, 2, 1>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          case 4: gather_cells<1, 1, 2>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          case 5: gather_cells<2, 1, 2>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          case 6: gather_cells<1, 2, 2>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
+          default: gather_cells<2, 2, 2>(rb, e0, sy, sz, idx, pos0, cy, cx, col, lane); break;
         }
         for (int e = lane; e < len; e += 32) {
           if (ovw) __stcs(row + e, rb[e]); else row[e] += rb[e];
         }
         __syncwarp();
-      }
-      // next node along x (carry into y, z)
-      if (++ix == g.nn[0]) {
-        ix = 0;
-        if (++iy == g.nn[1]) { iy = 0; ++iz; }
       }
     }
   }
