@@ -385,7 +385,10 @@ __device__ __forceinline__ void gather_cells(float* __restrict__ rb, const float
 // row with four shuffles: set-up that every lane used to repeat for every row was most of the kernel's
 // instructions.  A Q2 row's column range along an axis starts at the lowest node of its first cell, so a
 // lane's column position in the row depends only on the row's extents (cx, cy).
-__global__ void __launch_bounds__(GT) k_q2_gather(Grid g, int64_t nrows, const float* __restrict__ E,
+// 8 CTAs per SM (64 warps) by measurement: the kernel waits on memory latency, so occupancy pays more
+// than the 32-register cap costs (40 bytes of spills): C3 Jacobian 0.918 (no floor, 48 registers) ->
+// 0.877 (6 CTAs) -> 0.822 ms; two rows' loads in flight per warp at 62 registers was slower
+__global__ void __launch_bounds__(GT, 8) k_q2_gather(Grid g, int64_t nrows, const float* __restrict__ E,
                                                   float* __restrict__ J, int ovw) {
   __shared__ float rows[GT / 32][128];
   const int lane = threadIdx.x & 31;
