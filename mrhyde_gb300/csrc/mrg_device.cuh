@@ -253,14 +253,25 @@ __device__ __forceinline__ bool wbar_wait(uint32_t mbar, uint32_t parity) {
   return __all_sync(0xffffffffu, ok) != 0;
 }
 
-// Issues the copy of warp tile `tile` into buf; returns the global byte address mapped to buf[0].
+// Issues the copy of warp tile `tile` into buf; returns the global byte address mapped to buf[0].  R is
+// the set-up of the lane's row of the tile (kept until the tile is processed); the tile's CSR segment runs
+// from lane 0's row start to the end of its last row.
 template <typename JT>
 __device__ __forceinline__ uintptr_t wtile_issue(const Grid& g, int64_t nrows, const JT* __restrict__ J, int64_t tile,
-                                                 JT* buf, uint32_t mbar, int lane) {
+                                                 JT* buf, uint32_t mbar, int lane, RowInfo& R) {
   const int64_t n0 = tile * WROWS;
   const int64_t n1 = (n0 + WROWS < nrows) ? n0 + WROWS : nrows;
   const int64_t nnz = g.T[0] * g.T[1] * g.T[2];
-  const int64_t seg0 = row_ptr_at<1>(g, n0, nrows), seg1 = row_ptr_at<1>(g, n1, nrows);
+  int64_t rend = 0;
+  R = RowInfo{0, 0, 0, 1, 1, 1, 0};
+  if (n0 + lane < nrows) {
+    int ix, iy, iz;
+    decompose(g, n0 + lane, ix, iy, iz);
+    R = row_info<1>(g, ix, iy, iz);
+    rend = R.rp + (int64_t)R.cx * R.cy * R.cz;
+  }
+  const int64_t seg0 = __shfl_sync(0xffffffffu, R.rp, 0);
+  const int64_t seg1 = __shfl_sync(0xffffffffu, rend, (int)(n1 - n0) - 1);
   const uintptr_t lo = (uintptr_t)(J + seg0), hi = (uintptr_t)(J + seg1);
   const uintptr_t base = lo & ~(uintptr_t)15;
   const uintptr_t jb = ((uintptr_t)J + 15) & ~(uintptr_t)15, je = (uintptr_t)(J + nnz) & ~(uintptr_t)15;
@@ -314,15 +325,16 @@ __device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, c
   uint32_t ph0 = 0u, ph1 = 0u;
   bool armed0 = false, armed1 = false, ok = true;
   int b = 0;
+  RowInfo Rc, Rn;  // the lane's row of the current tile / of the next tile
   if (tile < ntiles) {
-    base0 = wtile_issue<JT>(g, nrows, J, tile, buf0, mb0, lane);
+    base0 = wtile_issue<JT>(g, nrows, J, tile, buf0, mb0, lane, Rc);
     armed0 = true;
   }
   for (; tile < ntiles; tile += W) {
     const int64_t nxt = tile + W;
     if (nxt < ntiles) {
-      if (b == 0) { base1 = wtile_issue<JT>(g, nrows, J, nxt, buf1, mb1, lane); armed1 = true; }
-      else        { base0 = wtile_issue<JT>(g, nrows, J, nxt, buf0, mb0, lane); armed0 = true; }
+      if (b == 0) { base1 = wtile_issue<JT>(g, nrows, J, nxt, buf1, mb1, lane, Rn); armed1 = true; }
+      else        { base0 = wtile_issue<JT>(g, nrows, J, nxt, buf0, mb0, lane, Rn); armed0 = true; }
     }
     const bool got = (b == 0) ? wbar_wait(mb0, ph0) : wbar_wait(mb1, ph1);
     if (!got) { ok = false; break; }
@@ -330,14 +342,12 @@ __device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, c
     __syncwarp();
     const int64_t n = tile * WROWS + lane;
     if (n < nrows) {
-      int ix, iy, iz;
-      decompose(g, n, ix, iy, iz);
-      const RowInfo R = row_info<1>(g, ix, iy, iz);
       const unsigned char* cb = reinterpret_cast<const unsigned char*>(b == 0 ? buf0 : buf1);
-      const JT* vals = reinterpret_cast<const JT*>(cb + ((uintptr_t)(J + R.rp) - (b == 0 ? base0 : base1)));
-      f(n, R, vals);
+      const JT* vals = reinterpret_cast<const JT*>(cb + ((uintptr_t)(J + Rc.rp) - (b == 0 ? base0 : base1)));
+      f(n, Rc, vals);
     }
     __syncwarp();
+    Rc = Rn;
     b ^= 1;
   }
   if (!ok) {  // let copies still in flight land before the CTA exits (bounded)
