@@ -215,8 +215,12 @@ enum { MRG_KRYLOV_AUTO = 0, MRG_KRYLOV_PCG = 1, MRG_KRYLOV_BICGSTAB = 2 };
                       Chebyshev-Jacobi smoothing, dense coarsest solve -- the structured-grid counterpart
                       of the reference's MueLu multigrid option for Belos
                       (src/interfaces/linear_algebra/linearAlgebraInterface_solvers.hpp:15-160).
-                      Q1 problems only (MRG_ENOTSUP for Q2).  Runs in the precision of the Jacobian. */
-enum { MRG_PREC_JACOBI = 0, MRG_PREC_GMG = 1 };
+                      Q1 and Q2 problems (a Q2 level 0 is coarsened to Q1 first; MRG_ENOTSUP for higher
+                      orders).  Runs in the precision of the Jacobian.
+                      In FP32 the levels of at most 1024 rows run as one single-CTA kernel per cycle.
+     MRG_PREC_GMG_SPLIT  the same cycle with every step of every level its own launch (bit-identical
+                      results; for comparison) */
+enum { MRG_PREC_JACOBI = 0, MRG_PREC_GMG = 1, MRG_PREC_GMG_SPLIT = 2 };
 int mrg_set_preconditioner(mrg_problem* p, int32_t kind);
 
 typedef struct mrg_newton_opts {

@@ -63,7 +63,7 @@ class SolveStats(C.Structure):
 
 
 MRG_KRYLOV_AUTO, MRG_KRYLOV_PCG, MRG_KRYLOV_BICGSTAB = 0, 1, 2
-MRG_PREC_JACOBI, MRG_PREC_GMG = 0, 1
+MRG_PREC_JACOBI, MRG_PREC_GMG, MRG_PREC_GMG_SPLIT = 0, 1, 2
 
 
 class NewtonOpts(C.Structure):

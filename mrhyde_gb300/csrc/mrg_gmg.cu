@@ -468,6 +468,32 @@ __global__ void k_cheb_coef(const unsigned int* __restrict__ lmax_bits, int nlev
   }
 }
 
+// Rounded operations that the compiler does not contract: the row updates shared by the per-step kernels
+// and k_vcycle_tail must round the same way in both.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// Chebyshev-Jacobi step k for row n given ax = (A x_in)_n: d = c_first z (k = 0) or c_old d + c_new z with
+// z = D^{-1} (b - ax); x_out = x_in + d (x_in = 0 when zero_x).  Shared by k_cheb and k_vcycle_tail.
+template <typename T>
+__device__ __forceinline__ void cheb_row(const LevDev<T>& L, int64_t n, T ax, const T* __restrict__ xin,
+                                         T* __restrict__ xout, int k, int zero_x, T c_first, T c_old, T c_new) {
+  const T z = mul_rn(L.minv[n], sub_rn(L.b[n], ax));
+  const T d = (k == 0) ? mul_rn(c_first, z) : fma(c_old, L.d[n], mul_rn(c_new, z));
+  L.d[n] = d;
+  xout[n] = add_rn(zero_x ? T(0) : xin[n], d);
+}
+
+// r = b - A x, row n
+template <typename T>
+__device__ __forceinline__ void resid_row(const LevDev<T>& L, int64_t n, T ax) {
+  L.r[n] = sub_rn(L.b[n], ax);
+}
+
 template <int P, typename T>
 __global__ void __launch_bounds__(NT) k_cheb(LevDev<T> L, const T* __restrict__ xin, T* __restrict__ xout, int k,
                                              int zero_x, const double* __restrict__ coef,
@@ -476,12 +502,7 @@ __global__ void __launch_bounds__(NT) k_cheb(LevDev<T> L, const T* __restrict__ 
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
   if (is_done(S)) return;
   const T c_first = (T)coef[3 * k], c_old = (T)coef[3 * k + 1], c_new = (T)coef[3 * k + 2];
-  auto fin = [&](int64_t n, T ax) {
-    const T z = L.minv[n] * (L.b[n] - ax);
-    const T d = (k == 0) ? c_first * z : c_old * L.d[n] + c_new * z;
-    L.d[n] = d;
-    xout[n] = (zero_x ? T(0) : xin[n]) + d;
-  };
+  auto fin = [&](int64_t n, T ax) { cheb_row<T>(L, n, ax, xin, xout, k, zero_x, c_first, c_old, c_new); };
   if (zero_x) {
     for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < L.n; n += (int64_t)gridDim.x * NT) fin(n, T(0));
     return;
@@ -500,7 +521,7 @@ __global__ void __launch_bounds__(NT) k_resid(LevDev<T> L, const T* __restrict__
   __shared__ __align__(8) uint64_t mbar[2 * (NT / 32)];
   if (is_done(S)) return;
   const bool ok = level_rows<P, T>(L.g, L.n, L.A, smem_raw, mbar, [&](int64_t n, const RowInfo& R, const T* vals) {
-    L.r[n] = L.b[n] - (T)row_prod<P, T>(L.g, R, vals, x);
+    resid_row<T>(L, n, (T)row_prod<P, T>(L.g, R, vals, x));
   });
   if (!ok) atomicExch(err, 3);
 }
@@ -546,16 +567,14 @@ __device__ __forceinline__ void parent_slots(int i, int nnf, int nnc, int co, bo
   }
 }
 
-// b_c = P^T r_f
+// b_c = P^T r_f, coarse row n (shared by k_restrict and k_vcycle_tail)
 template <typename T>
-__global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const T* __restrict__ rf, T* __restrict__ bc,
-                                                 const GScal* __restrict__ S) {
-  if (is_done(S)) return;
-  const int64_t nc = (int64_t)gc.nn[0] * gc.nn[1] * gc.nn[2];
-  for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < nc; n += (int64_t)gridDim.x * NT) {
+__device__ __forceinline__ void restrict_row(const Grid& gf, const Grid& gc, const Xfer& X, const T* __restrict__ rf,
+                                             T* __restrict__ bc, int64_t n) {
+  {
     int I[3];
     decompose(gc, n, I[0], I[1], I[2]);
-    if (node_fixed(gc, I[0], I[1], I[2])) { bc[n] = T(0); continue; }
+    if (node_fixed(gc, I[0], I[1], I[2])) { bc[n] = T(0); return; }
     int c0[3], c1[3], c2[3];
     float w0[3], w1[3], w2[3];
     bool k0[3], k1[3], k2[3];
@@ -572,22 +591,29 @@ __global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const
           if (!(k2[a2] && k1[a1] && k0[a0])) continue;
           const int ix = c0[a0], iy = c1[a1], iz = c2[a2];
           if (node_fixed(gf, ix, iy, iz)) continue;
-          s += (T)(w0[a0] * w1[a1] * w2[a2]) * rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)];
+          s = fma((T)(w0[a0] * w1[a1] * w2[a2]), rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)], s);
         }
     bc[n] = s;
   }
 }
 
-// x_f += P x_c
 template <typename T>
-__global__ void __launch_bounds__(NT) k_prolong(Grid gf, Grid gc, Xfer X, const T* __restrict__ xc, T* __restrict__ xf,
-                                                const GScal* __restrict__ S) {
+__global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const T* __restrict__ rf, T* __restrict__ bc,
+                                                 const GScal* __restrict__ S) {
   if (is_done(S)) return;
-  const int64_t nf = (int64_t)gf.nn[0] * gf.nn[1] * gf.nn[2];
-  for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < nf; n += (int64_t)gridDim.x * NT) {
+  const int64_t nc = (int64_t)gc.nn[0] * gc.nn[1] * gc.nn[2];
+  for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < nc; n += (int64_t)gridDim.x * NT)
+    restrict_row<T>(gf, gc, X, rf, bc, n);
+}
+
+// x_f += P x_c, fine row n (shared by k_prolong and k_vcycle_tail)
+template <typename T>
+__device__ __forceinline__ void prolong_row(const Grid& gf, const Grid& gc, const Xfer& X, const T* __restrict__ xc,
+                                            T* __restrict__ xf, int64_t n) {
+  {
     int i[3];
     decompose(gf, n, i[0], i[1], i[2]);
-    if (node_fixed(gf, i[0], i[1], i[2])) continue;
+    if (node_fixed(gf, i[0], i[1], i[2])) return;
     int p0[2], p1[2], p2[2];
     float w0[2], w1[2], w2[2];
     bool k0[2], k1[2], k2[2];
@@ -603,21 +629,109 @@ __global__ void __launch_bounds__(NT) k_prolong(Grid gf, Grid gc, Xfer X, const 
         for (int b0 = 0; b0 < 2; ++b0) {
           if (!(k2[b2] && k1[b1] && k0[b0])) continue;
           if (node_fixed(gc, p0[b0], p1[b1], p2[b2])) continue;
-          s += (T)(w0[b0] * w1[b1] * w2[b2]) * xc[p0[b0] + (int64_t)gc.nn[0] * (p1[b1] + (int64_t)gc.nn[1] * p2[b2])];
+          s = fma((T)(w0[b0] * w1[b1] * w2[b2]), xc[p0[b0] + (int64_t)gc.nn[0] * (p1[b1] + (int64_t)gc.nn[1] * p2[b2])], s);
         }
-    xf[n] += s;
+    xf[n] = add_rn(xf[n], s);
   }
 }
 
-// x = inv b on the coarsest level
+template <typename T>
+__global__ void __launch_bounds__(NT) k_prolong(Grid gf, Grid gc, Xfer X, const T* __restrict__ xc, T* __restrict__ xf,
+                                                const GScal* __restrict__ S) {
+  if (is_done(S)) return;
+  const int64_t nf = (int64_t)gf.nn[0] * gf.nn[1] * gf.nn[2];
+  for (int64_t n = (int64_t)blockIdx.x * NT + threadIdx.x; n < nf; n += (int64_t)gridDim.x * NT)
+    prolong_row<T>(gf, gc, X, xc, xf, n);
+}
+
+// x = inv b on the coarsest level, row i (shared by k_coarse_apply and k_vcycle_tail)
+template <typename T>
+__device__ __forceinline__ void coarse_row(int n, const T* __restrict__ inv, const T* __restrict__ b, T* __restrict__ x,
+                                           int i) {
+  T s = T(0);
+  for (int j = 0; j < n; ++j) s = fma(inv[i * n + j], b[j], s);
+  x[i] = s;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) k_coarse_apply(int n, const T* __restrict__ inv, const T* __restrict__ b,
                                                      T* __restrict__ x, const GScal* __restrict__ S) {
   if (is_done(S)) return;
-  for (int i = threadIdx.x; i < n; i += NT) {
-    T s = T(0);
-    for (int j = 0; j < n; ++j) s += inv[i * n + j] * b[j];
-    x[i] = s;
+  for (int i = threadIdx.x; i < n; i += NT) coarse_row<T>(n, inv, b, x, i);
+}
+
+// ---- the coarse end of the V-cycle in one CTA ---------------------------------------------------------
+// The smallest levels take a microsecond of work per step but a launch each (seven per level and cycle).
+// k_vcycle_tail runs the whole cycle below the first such level -- pre-smoothing, residual and restriction
+// down to the coarsest level, the dense coarsest solve, prolongation and post-smoothing back up -- in one
+// CTA, with a CTA barrier between steps.  Every row is computed by the same device functions, in the same
+// order, as by the per-step kernels, so the result is bit-identical (MRG_PREC_GMG_SPLIT keeps the per-step
+// launches for comparison).
+constexpr int TT = 1024;               // threads of the tail CTA
+constexpr int MAXTAIL = 8;             // levels the tail can hold
+constexpr int64_t TAIL_ROWS32 = 1024;  // FP32: first level taken into the tail has at most this many rows
+// A level's sweep in one SM must cost less than the launches it replaces.  Measured on the C2 mixed
+// multigrid Newton solve (128^3): FP32 tail from 9^3 nodes 9.62 ms, none 9.83 ms, from 17^3 nodes
+// 10.66 ms.  FP64 takes none: its pipe (1/64 of the FP32 rate) makes a single-SM sweep of a 729-row
+// level as long as a launch, and from 17^3 nodes the FP64 solve went 26.4 -> 31.9 ms.
+template <typename T>
+constexpr int64_t tail_rows() { return sizeof(T) == 4 ? TAIL_ROWS32 : 0; }
+
+template <typename T>
+struct TailArgs {
+  int nlev = 0;                  // levels in the tail; the last is the coarsest
+  LevDev<T> L[MAXTAIL];
+  Xfer X[MAXTAIL];               // X[j]: how tail level j was coarsened from level j - 1
+  const double* coef[MAXTAIL];   // Chebyshev coefficients of each level
+  const T* cinv = nullptr;       // dense inverse of the coarsest operator
+};
+
+template <typename T>
+__device__ __forceinline__ void tail_cheb(const LevDev<T>& D, const T* xin, T* xout, int k, int zero_x,
+                                          const double* __restrict__ coef) {
+  const T c_first = (T)coef[3 * k], c_old = (T)coef[3 * k + 1], c_new = (T)coef[3 * k + 2];
+  for (int64_t n = threadIdx.x; n < D.n; n += TT) {
+    T ax = T(0);
+    if (!zero_x) {
+      int ix, iy, iz;
+      decompose(D.g, n, ix, iy, iz);
+      const RowInfo R = row_info<1>(D.g, ix, iy, iz);
+      ax = (T)row_prod<1, T>(D.g, R, D.A + R.rp, xin);
+    }
+    cheb_row<T>(D, n, ax, xin, xout, k, zero_x, c_first, c_old, c_new);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TT) k_vcycle_tail(const TailArgs<T> A, const GScal* __restrict__ S) {
+  if (is_done(S)) return;
+  const int nl = A.nlev;
+  for (int j = 0; j < nl - 1; ++j) {
+    const LevDev<T>& D = A.L[j];
+    tail_cheb<T>(D, D.xa, D.xa, 0, 1, A.coef[j]);
+    tail_cheb<T>(D, D.xa, D.xb, 1, 0, A.coef[j]);
+    for (int64_t n = threadIdx.x; n < D.n; n += TT) {
+      int ix, iy, iz;
+      decompose(D.g, n, ix, iy, iz);
+      const RowInfo R = row_info<1>(D.g, ix, iy, iz);
+      resid_row<T>(D, n, (T)row_prod<1, T>(D.g, R, D.A + R.rp, D.xb));
+    }
+    __syncthreads();
+    const LevDev<T>& C = A.L[j + 1];
+    for (int64_t n = threadIdx.x; n < C.n; n += TT) restrict_row<T>(D.g, C.g, A.X[j + 1], D.r, C.b, n);
+    __syncthreads();
+  }
+  const LevDev<T>& Lc = A.L[nl - 1];
+  for (int i = threadIdx.x; i < (int)Lc.n; i += TT) coarse_row<T>((int)Lc.n, A.cinv, Lc.b, Lc.xb, i);
+  __syncthreads();
+  for (int j = nl - 2; j >= 0; --j) {
+    const LevDev<T>& D = A.L[j];
+    const LevDev<T>& C = A.L[j + 1];
+    for (int64_t n = threadIdx.x; n < D.n; n += TT) prolong_row<T>(D.g, C.g, A.X[j + 1], C.xb, D.xb, n);
+    __syncthreads();
+    tail_cheb<T>(D, D.xb, D.xa, 0, 0, A.coef[j]);
+    tail_cheb<T>(D, D.xa, D.xb, 1, 0, A.coef[j]);
   }
 }
 
@@ -927,10 +1041,15 @@ struct Hier {
   const void* bgraph_A = nullptr;
   cudaStream_t bgraph_stream = nullptr;
   const void* setup_J = nullptr;  // Jacobian of the last setup
+  // levels >= tail run in k_vcycle_tail (tail == number of levels: every step its own launch)
+  int tail = -1;
+  int graph_tail = -1, bgraph_tail = -1;  // the tail the captured chunks were recorded with
+  TailArgs<T> targs;
 };
 
 struct GmgData {
   int kind = MRG_PREC_JACOBI;
+  bool split = false;  // MRG_PREC_GMG_SPLIT: no fused coarse-level tail
   Hier<double>* h64 = nullptr;
   Hier<float>* h32 = nullptr;
 };
@@ -1098,6 +1217,31 @@ LevDev<T> levdev(const HLevel& L) {
   return LevDev<T>{L.g, L.n, (const T*)L.A, (T*)L.minv, (T*)L.xa, (T*)L.xb, (T*)L.d, (T*)L.b, (T*)L.r};
 }
 
+// First level of the fused tail: the first level below the finest with at most tail_rows<T>() rows (all
+// levels below the finest are Q1), unless the caller asked for the split cycle or the tail would be too
+// deep.  Fills the tail's kernel arguments.
+template <typename T>
+void set_tail(Hier<T>* H, bool split) {
+  const int nl = (int)H->L.size();
+  int t = nl;
+  if (!split) {
+    for (int l = 1; l < nl; ++l)
+      if (H->L[l].n <= tail_rows<T>()) { t = l; break; }
+    if (nl - t > MAXTAIL) t = nl;
+    for (int l = t; l < nl; ++l)
+      if (H->L[l].pp.p[0] != 1 || H->L[l].pp.p[1] != 1 || H->L[l].pp.p[2] != 1) t = nl;
+  }
+  H->tail = t;
+  TailArgs<T>& A = H->targs;
+  A.nlev = nl - t;
+  for (int j = 0; j < A.nlev; ++j) {
+    A.L[j] = levdev<T>(H->L[t + j]);
+    A.X[j] = H->L[t + j].X;
+    A.coef[j] = H->coef + (size_t)(t + j) * NU * 3;
+  }
+  A.cinv = H->cinv;
+}
+
 template <typename T>
 int set_staged_attr() {
   static std::once_flag once;
@@ -1182,8 +1326,9 @@ void launch_resid(const HLevel& L, const LevDev<T>& D, const T* x, const GScal* 
 template <typename T>
 void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
   const int nl = (int)H->L.size();
+  const int tail = H->tail < 1 ? nl : H->tail;  // levels >= tail: k_vcycle_tail
   const GScal* S = H->S;
-  for (int l = 0; l < nl - 1; ++l) {
+  for (int l = 0; l < nl - 1 && l < tail; ++l) {
     LevDev<T> D = levdev<T>(H->L[l]);
     if (l == 0) D.b = const_cast<T*>(in);
     // pre-smoothing from x = 0: xa <- step 0, xb <- step 1
@@ -1193,9 +1338,13 @@ void enqueue_vcycle(Hier<T>* H, const T* in, T* out, cudaStream_t s) {
     const HLevel& C = H->L[l + 1];
     k_restrict<T><<<grid_for(C.n, 16), NT, 0, s>>>(D.g, C.g, C.X, D.r, (T*)C.b, S);
   }
-  const HLevel& Lc = H->L[nl - 1];
-  k_coarse_apply<T><<<1, NT, 0, s>>>((int)Lc.n, H->cinv, (const T*)Lc.b, (T*)Lc.xb, S);
-  for (int l = nl - 2; l >= 0; --l) {
+  if (tail < nl) {
+    k_vcycle_tail<T><<<1, TT, 0, s>>>(H->targs, S);
+  } else {
+    const HLevel& Lc = H->L[nl - 1];
+    k_coarse_apply<T><<<1, NT, 0, s>>>((int)Lc.n, H->cinv, (const T*)Lc.b, (T*)Lc.xb, S);
+  }
+  for (int l = std::min(tail, nl - 1) - 1; l >= 0; --l) {
     LevDev<T> D = levdev<T>(H->L[l]);
     if (l == 0) D.b = const_cast<T*>(in);
     const HLevel& C = H->L[l + 1];
@@ -1270,6 +1419,7 @@ int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, d
     if (rc) return rc;
     H->setup_J = J;
   }
+  set_tail(H, gdata(p)->split);
   GScal init{};
   init.tol = rtol;
   init.maxiter = maxiter;
@@ -1282,7 +1432,7 @@ int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, d
   k_cg_rz<T><<<grid_for(n, 16), NT, 0, s>>>(n, V, 1);
   MRG_CUDA(cudaGetLastError());
   // captured chunk of iterations (re-captured when the Jacobian pointer or the stream changes)
-  if (!H->graph || H->graph_A != (const void*)J || H->graph_stream != s) {
+  if (!H->graph || H->graph_A != (const void*)J || H->graph_stream != s || H->graph_tail != H->tail) {
     if (H->graph) {
       cudaGraphExecDestroy(H->graph);
       H->graph = nullptr;
@@ -1301,6 +1451,7 @@ int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, d
     if (e != cudaSuccess) return mrg_cuda_check(e, "multigrid CG graph capture");
     H->graph_A = J;
     H->graph_stream = s;
+    H->graph_tail = H->tail;
   }
   return finish_solve(p, H, H->graph, x, rtol, maxiter, st, s, "multigrid CG");
 }
@@ -1343,13 +1494,14 @@ int gmg_bicgstab(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double
     if (rc) return rc;
     H->setup_J = J;
   }
+  set_tail(H, gdata(p)->split);
   GScal init{};
   init.tol = rtol;
   init.maxiter = maxiter;
   MRG_CUDA(cudaMemcpyAsync(H->S, &init, sizeof(GScal), cudaMemcpyHostToDevice, s));
   k_bg_init<T><<<grid_for(n, 16), NT, 0, s>>>(n, b, bgvec(H));
   MRG_CUDA(cudaGetLastError());
-  if (!H->bgraph || H->bgraph_A != (const void*)J || H->bgraph_stream != s) {
+  if (!H->bgraph || H->bgraph_A != (const void*)J || H->bgraph_stream != s || H->bgraph_tail != H->tail) {
     if (H->bgraph) {
       cudaGraphExecDestroy(H->bgraph);
       H->bgraph = nullptr;
@@ -1368,6 +1520,7 @@ int gmg_bicgstab(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double
     if (e != cudaSuccess) return mrg_cuda_check(e, "multigrid BiCGStab graph capture");
     H->bgraph_A = J;
     H->bgraph_stream = s;
+    H->bgraph_tail = H->tail;
   }
   return finish_solve(p, H, H->bgraph, x, rtol, maxiter, st, s, "multigrid BiCGStab");
 }
@@ -1418,9 +1571,11 @@ int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, 
 
 extern "C" int mrg_set_preconditioner(mrg_problem* p, int32_t kind) {
   if (!p) return mrg_fail(MRG_EINVAL, "mrg_set_preconditioner: null problem");
-  if (kind != MRG_PREC_JACOBI && kind != MRG_PREC_GMG)
+  if (kind != MRG_PREC_JACOBI && kind != MRG_PREC_GMG && kind != MRG_PREC_GMG_SPLIT)
     return mrg_fail(MRG_EINVAL, "mrg_set_preconditioner: unknown preconditioner");
-  if (kind == MRG_PREC_GMG && p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid preconditioner: Q1 and Q2 problems only");
-  gdata(p)->kind = kind;
+  if (kind != MRG_PREC_JACOBI && p->g.p > 2)
+    return mrg_fail(MRG_ENOTSUP, "multigrid preconditioner: Q1 and Q2 problems only");
+  gdata(p)->kind = (kind == MRG_PREC_GMG_SPLIT) ? MRG_PREC_GMG : kind;
+  gdata(p)->split = (kind == MRG_PREC_GMG_SPLIT);
   return MRG_OK;
 }

@@ -42,11 +42,13 @@ class SolverManager:
         self.mixed = mixed_precision
         self.reuse_jacobian = reuse_jacobian
         self.krylov = {"auto": L.MRG_KRYLOV_AUTO, "pcg": L.MRG_KRYLOV_PCG, "bicgstab": L.MRG_KRYLOV_BICGSTAB}[krylov]
-        # "jacobi": the reference's SolverManager::PCG; "gmg": geometric multigrid V-cycle (Q1 only), the
-        # structured-grid counterpart of the reference's Belos + MueLu option.  The choice is a property
-        # of the problem handle (mrg_set_preconditioner) and applies to PCG and to Newton's CG.
+        # "jacobi": the reference's SolverManager::PCG; "gmg": geometric multigrid V-cycle (Q1 and Q2),
+        # the structured-grid counterpart of the reference's Belos + MueLu option; "gmg_split": the same
+        # cycle with every coarse-level step its own launch (bit-identical, for comparison).  The choice
+        # is a property of the problem handle (mrg_set_preconditioner) and applies to PCG, BiCGStab and
+        # Newton's Krylov solves.
         self.preconditioner = preconditioner
-        prec = {"jacobi": L.MRG_PREC_JACOBI, "gmg": L.MRG_PREC_GMG}[preconditioner]
+        prec = {"jacobi": L.MRG_PREC_JACOBI, "gmg": L.MRG_PREC_GMG, "gmg_split": L.MRG_PREC_GMG_SPLIT}[preconditioner]
         L.check(L.lib().mrg_set_preconditioner(problem.handle, prec), "mrg_set_preconditioner")
 
     def setDirichlet(self, u: torch.Tensor, stream=None):

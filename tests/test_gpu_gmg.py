@@ -223,3 +223,53 @@ def test_assembly_is_graph_capturable(cuda, order, fp32):
     g.replay()
     torch.cuda.synchronize()
     assert torch.equal(r1, r2) and torch.equal(J1, J2)
+
+
+# FP32 hierarchies run their levels of at most 1024 rows in one single-CTA kernel per cycle by default, and
+# as one launch per step with "gmg_split": the same rows by the same device functions in the same order, so
+# the iterates agree to the last bit.  The grids put the first fused FP32 level at depth 2 (3-D) and 1
+# (2-D).  FP64 hierarchies keep the per-step launches in both settings.
+TAIL_CFGS = [CFGS[0], CFGS[3], dict(dim=3, order=1, n=(40, 36, 32), dirichlet_faces=3)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg", TAIL_CFGS, ids=[f"n{'x'.join(map(str, c['n']))}" for c in TAIL_CFGS])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_fused_coarse_tail_pcg_bit_identical(cuda, cfg, fp32):
+    from mrhyde_gb300 import AssemblyManager, SolverManager
+
+    c = _with_kappa(cfg, 11)
+    G = gpu_problem(c)
+    A = AssemblyManager(G)
+    r, J = G.new_vector(), G.new_matrix_values(fp32=fp32)
+    A.assembleJacRes(G.new_vector(), r, J, fp32_jacobian=fp32, overwrite=True)
+    out = {}
+    for prec in ("gmg", "gmg_split", "gmg"):  # and back: the captured chunk follows the setting
+        S = SolverManager(G, preconditioner=prec)
+        x = G.new_vector()
+        res = S.PCG(J, r, x, tol=1e-5 if fp32 else 1e-11, maxiter=200)
+        out.setdefault(prec, []).append((x.cpu(), res.iterations, res.rel_residual))
+    runs = out["gmg"] + out["gmg_split"]
+    for x, it, rel in runs[1:]:
+        assert it == runs[0][1] and rel == runs[0][2]
+        assert torch.equal(x, runs[0][0])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2])
+def test_fused_coarse_tail_bicgstab_newton_bit_identical(cuda, order):
+    from mrhyde_gb300 import SolverManager
+
+    n = (16, 12, 10) if order == 1 else (6, 5, 4)
+    cfg = dict(dim=3, order=order, n=n, kind="diffusion_1pu2", dirichlet_faces=3, source=("const", 10.0, 0.0))
+    us = []
+    for prec in ("gmg", "gmg_split"):
+        G = gpu_problem(cfg)
+        S = SolverManager(G, nonlinear_tol=1e-10, max_nonlinear_iters=20, linear_tol=1e-4, mixed_precision=True,
+                          preconditioner=prec)
+        u = G.new_vector()
+        res = S.nonlinearSolver(u)
+        assert res.rel_residual < 1e-10
+        us.append((u.cpu(), res.iterations, res.outer_iterations))
+    assert us[0][1:] == us[1][1:]
+    assert torch.equal(us[0][0], us[1][0])
