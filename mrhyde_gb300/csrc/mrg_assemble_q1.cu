@@ -330,52 +330,64 @@ __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const 
       for (int c = 0; c < 8; ++c) t[c] = 0.0;
       float osum = 0.0f, ocomp = 0.0f;
       int dpos = 0;
-      int pos = 0;
       const int64_t plane = (int64_t)NX * NY;
       bool ubad = false;  // ZAX: a skipped residual term is NaN (FP64 and mixed)
-#pragma unroll
-      for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx)
-            if (vz[dz + 1] && vy[dy + 1] && vx[dx + 1]) {
-              const int cls = (dx != 0) + 2 * (dy != 0) + 4 * (dz != 0);
-              const double s = S[dz + 1][dy + 1][dx + 1];
-              if (!MIXED) {
-                if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
-                  // K = +0: the product +0 * s is a zero with the sign of s (NaN for a non-finite s), and
-                  // the residual term -(+-0) * u leaves acc unchanged unless s or u is not finite (then
-                  // NaN).  No FP64 instruction: on cubic cells 12 of an interior row's 54.
-                  const bool sbad = nonfinite(s);
-                  if (DOJ)
-                    sv[loc + pos] = (JT)__longlong_as_double(
-                        sbad ? 0x7fffffffffffffffll : (long long)((unsigned long long)__double_as_longlong(s) & 0x8000000000000000ull));
-                  if (DOR) ubad |= sbad | nonfinite(__ldg(u + n + dx + (int64_t)NX * dy + plane * dz));
-                } else {
-                  const double a = A.Kp[cls] * s;
-                  if (DOJ) sv[loc + pos] = (JT)a;
-                  if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
-                }
-              } else {
-                if (DOJ) {
-                  if (cls == 0) {
-                    dpos = pos;
-                  } else {
-                    const float v = A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1];
-                    sv[loc + pos] = (JT)v;
-                    neumaier_add(osum, ocomp, v);
-                  }
-                }
-                if (DOR) {
-                  const double uv = __ldg(u + n + dx + (int64_t)NX * dy + plane * dz);
-                  // K = +0 class: K * t is +0 unless S or u is not finite (the same rule as FP64 above)
-                  if (ZAX && (cls == 1 || cls == 2 || cls == 4)) ubad |= nonfinite(s) | nonfinite(uv);
-                  else t[cls] = fma(s, uv, t[cls]);
-                }
-              }
-              ++pos;
+      // entry (dz, dy, dx) at position pos of the row
+      auto entry = [&](const int dz, const int dy, const int dx, const int pos) {
+        const int cls = (dx != 0) + 2 * (dy != 0) + 4 * (dz != 0);
+        const double s = S[dz + 1][dy + 1][dx + 1];
+        if (!MIXED) {
+          if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
+            // K = +0: the product +0 * s is a zero with the sign of s (NaN for a non-finite s), and the
+            // residual term -(+-0) * u leaves acc unchanged unless s or u is not finite (then NaN).  No FP64
+            // instruction: on cubic cells 12 of an interior row's 54.
+            const bool sbad = nonfinite(s);
+            if (DOJ)
+              sv[loc + pos] = (JT)__longlong_as_double(
+                  sbad ? 0x7fffffffffffffffll : (long long)((unsigned long long)__double_as_longlong(s) & 0x8000000000000000ull));
+            if (DOR) ubad |= sbad | nonfinite(__ldg(u + n + dx + (int64_t)NX * dy + plane * dz));
+          } else {
+            const double a = A.Kp[cls] * s;
+            if (DOJ) sv[loc + pos] = (JT)a;
+            if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+          }
+        } else {
+          if (DOJ) {
+            if (cls == 0) {
+              dpos = pos;
+            } else {
+              const float v = A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1];
+              sv[loc + pos] = (JT)v;
+              neumaier_add(osum, ocomp, v);
             }
+          }
+          if (DOR) {
+            const double uv = __ldg(u + n + dx + (int64_t)NX * dy + plane * dz);
+            // K = +0 class: K * t is +0 unless S or u is not finite (the same rule as FP64 above)
+            if (ZAX && (cls == 1 || cls == 2 || cls == 4)) ubad |= nonfinite(s) | nonfinite(uv);
+            else t[cls] = fma(s, uv, t[cls]);
+          }
+        }
+      };
+      if (DOJ && cx == 3 && cy == 3 && cz == 3) {
+        // interior row: all 27 entries, their positions in the staged row known at compile time (the
+        // residual-only instances keep the single loop: there it measured 5 % slower)
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+          for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) entry(dz, dy, dx, (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
+      } else {
+        int pos = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+          for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx)
+              if (vz[dz + 1] && vy[dy + 1] && vx[dx + 1]) entry(dz, dy, dx, pos++);
+      }
       if (MIXED && DOJ) sv[loc + dpos] = (JT)(-(osum + ocomp));
       if (DOR) {
         if (MIXED) {
