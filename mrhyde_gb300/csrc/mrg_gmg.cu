@@ -571,30 +571,28 @@ __device__ __forceinline__ void parent_slots(int i, int nnf, int nnc, int co, bo
 template <typename T>
 __device__ __forceinline__ void restrict_row(const Grid& gf, const Grid& gc, const Xfer& X, const T* __restrict__ rf,
                                              T* __restrict__ bc, int64_t n) {
-  {
-    int I[3];
-    decompose(gc, n, I[0], I[1], I[2]);
-    if (node_fixed(gc, I[0], I[1], I[2])) { bc[n] = T(0); return; }
-    int c0[3], c1[3], c2[3];
-    float w0[3], w1[3], w2[3];
-    bool k0[3], k1[3], k2[3];
-    child_slots(I[0], gf.nn[0], gc.nn[0], X.co[0], gf.dim > 0, c0, w0, k0);
-    child_slots(I[1], gf.nn[1], gc.nn[1], X.co[1], gf.dim > 1, c1, w1, k1);
-    child_slots(I[2], gf.nn[2], gc.nn[2], X.co[2], gf.dim > 2, c2, w2, k2);
-    T s = T(0);
+  int I[3];
+  decompose(gc, n, I[0], I[1], I[2]);
+  if (node_fixed(gc, I[0], I[1], I[2])) { bc[n] = T(0); return; }
+  int c0[3], c1[3], c2[3];
+  float w0[3], w1[3], w2[3];
+  bool k0[3], k1[3], k2[3];
+  child_slots(I[0], gf.nn[0], gc.nn[0], X.co[0], gf.dim > 0, c0, w0, k0);
+  child_slots(I[1], gf.nn[1], gc.nn[1], X.co[1], gf.dim > 1, c1, w1, k1);
+  child_slots(I[2], gf.nn[2], gc.nn[2], X.co[2], gf.dim > 2, c2, w2, k2);
+  T s = T(0);
 #pragma unroll
-    for (int a2 = 0; a2 < 3; ++a2)
+  for (int a2 = 0; a2 < 3; ++a2)
 #pragma unroll
-      for (int a1 = 0; a1 < 3; ++a1)
+    for (int a1 = 0; a1 < 3; ++a1)
 #pragma unroll
-        for (int a0 = 0; a0 < 3; ++a0) {
-          if (!(k2[a2] && k1[a1] && k0[a0])) continue;
-          const int ix = c0[a0], iy = c1[a1], iz = c2[a2];
-          if (node_fixed(gf, ix, iy, iz)) continue;
-          s = fma((T)(w0[a0] * w1[a1] * w2[a2]), rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)], s);
-        }
-    bc[n] = s;
-  }
+      for (int a0 = 0; a0 < 3; ++a0) {
+        if (!(k2[a2] && k1[a1] && k0[a0])) continue;
+        const int ix = c0[a0], iy = c1[a1], iz = c2[a2];
+        if (node_fixed(gf, ix, iy, iz)) continue;
+        s = fma((T)(w0[a0] * w1[a1] * w2[a2]), rf[ix + (int64_t)gf.nn[0] * (iy + (int64_t)gf.nn[1] * iz)], s);
+      }
+  bc[n] = s;
 }
 
 template <typename T>
@@ -610,29 +608,27 @@ __global__ void __launch_bounds__(NT) k_restrict(Grid gf, Grid gc, Xfer X, const
 template <typename T>
 __device__ __forceinline__ void prolong_row(const Grid& gf, const Grid& gc, const Xfer& X, const T* __restrict__ xc,
                                             T* __restrict__ xf, int64_t n) {
-  {
-    int i[3];
-    decompose(gf, n, i[0], i[1], i[2]);
-    if (node_fixed(gf, i[0], i[1], i[2])) return;
-    int p0[2], p1[2], p2[2];
-    float w0[2], w1[2], w2[2];
-    bool k0[2], k1[2], k2[2];
-    parent_slots(i[0], gf.nn[0], gc.nn[0], X.co[0], gf.dim > 0, p0, w0, k0);
-    parent_slots(i[1], gf.nn[1], gc.nn[1], X.co[1], gf.dim > 1, p1, w1, k1);
-    parent_slots(i[2], gf.nn[2], gc.nn[2], X.co[2], gf.dim > 2, p2, w2, k2);
-    T s = T(0);
+  int i[3];
+  decompose(gf, n, i[0], i[1], i[2]);
+  if (node_fixed(gf, i[0], i[1], i[2])) return;
+  int p0[2], p1[2], p2[2];
+  float w0[2], w1[2], w2[2];
+  bool k0[2], k1[2], k2[2];
+  parent_slots(i[0], gf.nn[0], gc.nn[0], X.co[0], gf.dim > 0, p0, w0, k0);
+  parent_slots(i[1], gf.nn[1], gc.nn[1], X.co[1], gf.dim > 1, p1, w1, k1);
+  parent_slots(i[2], gf.nn[2], gc.nn[2], X.co[2], gf.dim > 2, p2, w2, k2);
+  T s = T(0);
 #pragma unroll
-    for (int b2 = 0; b2 < 2; ++b2)
+  for (int b2 = 0; b2 < 2; ++b2)
 #pragma unroll
-      for (int b1 = 0; b1 < 2; ++b1)
+    for (int b1 = 0; b1 < 2; ++b1)
 #pragma unroll
-        for (int b0 = 0; b0 < 2; ++b0) {
-          if (!(k2[b2] && k1[b1] && k0[b0])) continue;
-          if (node_fixed(gc, p0[b0], p1[b1], p2[b2])) continue;
-          s = fma((T)(w0[b0] * w1[b1] * w2[b2]), xc[p0[b0] + (int64_t)gc.nn[0] * (p1[b1] + (int64_t)gc.nn[1] * p2[b2])], s);
-        }
-    xf[n] = add_rn(xf[n], s);
-  }
+      for (int b0 = 0; b0 < 2; ++b0) {
+        if (!(k2[b2] && k1[b1] && k0[b0])) continue;
+        if (node_fixed(gc, p0[b0], p1[b1], p2[b2])) continue;
+        s = fma((T)(w0[b0] * w1[b1] * w2[b2]), xc[p0[b0] + (int64_t)gc.nn[0] * (p1[b1] + (int64_t)gc.nn[1] * p2[b2])], s);
+      }
+  xf[n] = add_rn(xf[n], s);
 }
 
 template <typename T>
