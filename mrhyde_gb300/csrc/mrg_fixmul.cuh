@@ -37,4 +37,25 @@ __host__ __device__ __forceinline__ uint64_t fix_to_f64_bits(uint64_t s, int ema
   return (e1 << 52) + ((s + bias) >> sh);
 }
 
+// RN(k * s) as an FP64 bit pattern (magnitude only) for two positive normal doubles given by their 53-bit
+// significands (implicit bit set) mk, ms and the sum of their biased exponents: the exact 106-bit product
+// from four 32 x 32-bit partial products, rounded once to nearest, ties to even -- the bits an FP64
+// multiply returns.  Requires a normal result: 1 <= ek + es - 1023 (+1) <= 2046, checked by the caller.
+__host__ __device__ __forceinline__ uint64_t mul_bits(uint64_t mk, uint64_t ms, int esum) {
+  const uint64_t kl = mk & 0xffffffffull, kh = mk >> 32, sl = ms & 0xffffffffull, sh = ms >> 32;
+  const uint64_t lo = kl * sl;
+  const uint64_t mid = kl * sh + kh * sl;  // < 2^54
+  const uint64_t plo = lo + (mid << 32);
+  const uint64_t phi = kh * sh + (mid >> 32) + (plo < lo ? 1u : 0u);
+  // product = phi 2^64 + plo in [2^104, 2^106); keep its top 53 bits
+  const bool top = (phi >> 41) != 0;
+  uint64_t m = top ? (phi << 11) | (plo >> 53) : (phi << 12) | (plo >> 52);
+  const uint64_t rem = top ? (plo & ((1ull << 53) - 1)) : (plo & ((1ull << 52) - 1));
+  const uint64_t half = top ? (1ull << 52) : (1ull << 51);
+  m += (rem > half || (rem == half && (m & 1u))) ? 1u : 0u;
+  // m in [2^52, 2^53]: adding it to (E - 1) << 52 sets the exponent field E (a carry to 2^53 moves into it)
+  const uint64_t E = (uint64_t)(esum - 1023 + (top ? 1 : 0));
+  return ((E - 1) << 52) + m;
+}
+
 }  // namespace mrgfix

@@ -226,3 +226,31 @@ def test_cube_mixed_j32_unchanged_and_residual():
     r_fx, _ = _assemble(G, u, native=False, fp32=True)
     r_nat, _ = _assemble(G, u, native=True, fp32=True)
     assert np.array_equal(np.isnan(r_fx), np.isnan(r_nat)) and np.isnan(r_fx).sum() > 1
+
+
+@pytest.mark.parametrize("hi", [(0.8, 0.7, 0.6), (1.0, 0.37, 2.5), (1e4, 1e4, 1e4)])  # cubic cells, boxes, huge h
+def test_residual_only_corner_products_bit_identical(hi):
+    # the residual-only pass forms the corner products K * kappa on the integer pipes: the same bits as the
+    # FP64 multiply of the Jacobian pass and of the native path, including zero kappa (a -0 product), a block
+    # of kappa near the top of the exact-sum range (rows inside it keep the integer products) and, on the
+    # coarse grid (h = 1250), products that would overflow (those rows take the multiply: inf)
+    n = (8, 7, 6)
+    kap = np.random.default_rng(18).integers(1, 9, n[0] * n[1] * n[2]).astype(np.float64)
+    K = kap.reshape(n[2], n[1], n[0])
+    K[1:4, 2:5, 3:6] = 1.7e306 * (1.0 + np.arange(27).reshape(3, 3, 3) % 3)
+    K[4, 5, 6] = 0.0
+    K[0, 0, 0] = 1e-300
+    G = gpu_problem(_cfg(kap, n, hi))
+    u = _u(G, 19)
+    r_res, _ = _assemble(G, u, native=False, jac=False)
+    r_jr, _ = _assemble(G, u, native=False)
+    r_nat, _ = _assemble(G, u, native=True, jac=False)
+    assert np.array_equal(r_res, r_jr, equal_nan=True)
+    assert np.array_equal(r_res, r_nat, equal_nan=True)
+    if hi[0] > 100:
+        assert np.isinf(r_res).any() or np.isnan(r_res).any()
+    kap2 = np.exp(np.random.default_rng(20).standard_normal(n[0] * n[1] * n[2]))
+    G2 = gpu_problem(_cfg(kap2, n, hi))
+    r_res, _ = _assemble(G2, u, native=False, jac=False)
+    r_jr, _ = _assemble(G2, u, native=False)
+    assert np.array_equal(r_res, r_jr)
