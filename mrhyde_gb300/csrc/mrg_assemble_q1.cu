@@ -121,8 +121,11 @@ struct FactArgs {
 // ------------------------------------------------------------------------------------------------
 // (1) factored row-gather, hexahedra.  JT = double (FP64 mode) or float (mixed mode).
 // ------------------------------------------------------------------------------------------------
-// Occupancy floors chosen by measurement: FP64 Jacobians 6 CTAs per SM (80 registers, no spills; 0.266 ->
-// 0.253 ms on C2), FP32 Jacobians 5 (96 registers; 0.252 -> 0.232 ms against the compiler's 117)
+// Occupancy floors chosen by measurement: FP64 Jacobians 6 CTAs per SM (80 registers; 0.266 -> 0.253 ms on
+// C2 when introduced; 7 and 8 CTAs, i.e. 72 and 64 registers, spilled more and were slower), FP32 Jacobians
+// 5 (96 registers; 0.252 -> 0.232 ms against the compiler's 117).  The interior-row path of the Jacobian
+// instances spills a few words at this floor and is still faster (FP64 0.201 -> 0.1996 ms, mixed
+// 0.189 -> 0.165 ms).
 template <typename JT, bool DOJ, bool DOR, bool OVW, bool ZAX>
 __global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const FactArgs A, const double* __restrict__ u,
                                                   const double* __restrict__ kap, const float* __restrict__ kap32,
