@@ -125,9 +125,10 @@ struct FactArgs {
 // C2 when introduced; 7 and 8 CTAs, i.e. 72 and 64 registers, spilled more and were slower), FP32 Jacobians
 // 5 (96 registers; 0.252 -> 0.232 ms against the compiler's 117).  The interior-row path of the Jacobian
 // instances spills a few words at this floor and is still faster (FP64 0.201 -> 0.1996 ms, mixed
-// 0.189 -> 0.165 ms).
+// 0.189 -> 0.165 ms).  Residual-only instances (no staged row in shared memory): 8 CTAs per SM, 64
+// registers with spills, 0.167 -> 0.156 ms (7 CTAs: 0.158 ms).
 template <typename JT, bool DOJ, bool DOR, bool OVW, bool ZAX>
-__global__ void __launch_bounds__(FT, sizeof(JT) == 8 ? 6 : 5) k_fact_hex(const FactArgs A, const double* __restrict__ u,
+__global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? 6 : 5)) k_fact_hex(const FactArgs A, const double* __restrict__ u,
                                                   const double* __restrict__ kap, const float* __restrict__ kap32,
                                                   double* __restrict__ r, JT* __restrict__ J) {
   constexpr bool MIXED = sizeof(JT) == 4;
