@@ -1,0 +1,33 @@
+"""Host logic of bench.py's roofline: the FP64 instruction count of the factored Q1 Jacobian+residual launch,
+against a brute-force enumeration of the free rows' entries (a multiply and an FMA per entry, none for the
+axis-neighbour entries of cubic cells, whose coefficient is +0; rows on x = 0 and x = 1 are Dirichlet)."""
+import itertools
+
+import pytest
+
+import bench
+
+
+def _brute(n, hi):
+    nn = [c + 1 for c in n]
+    h = [hi[k] / n[k] for k in range(3)]
+    cubic = h[0] == h[1] == h[2]
+    count = 0
+    for iz, iy, ix in itertools.product(range(nn[2]), range(nn[1]), range(nn[0])):
+        if ix == 0 or ix == nn[0] - 1:
+            continue
+        for dz, dy, dx in itertools.product((-1, 0, 1), repeat=3):
+            jx, jy, jz = ix + dx, iy + dy, iz + dz
+            if not (0 <= jx < nn[0] and 0 <= jy < nn[1] and 0 <= jz < nn[2]):
+                continue
+            if cubic and (dx != 0) + (dy != 0) + (dz != 0) == 1:
+                continue
+            count += 2
+    return count
+
+
+@pytest.mark.parametrize("n,hi", [((4, 4, 4), (1.0, 1.0, 1.0)), ((5, 3, 4), (1.0, 1.0, 1.0)),
+                                  ((6, 6, 6), (0.5, 0.5, 0.5)), ((3, 7, 2), (0.3, 0.7, 0.2))])
+def test_fp64_instruction_count(n, hi):
+    cfg = dict(n=n, lo=(0.0, 0.0, 0.0), hi=hi)
+    assert bench.fp64_instructions(cfg) == _brute(n, hi)
