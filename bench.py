@@ -18,7 +18,6 @@ import argparse
 import json
 import math
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -52,14 +51,12 @@ def read_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def read_profile_traffic(name):
-    """traffic (bytes/launch) recorded from an ncu capture in profiles/<name>.md (line 'traffic_bytes_per_launch: X')."""
-    path = os.path.join(ROOT, "profiles", name + ".md")
-    try:
-        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
-        return float(m.group(1)) if m else None
-    except Exception:
-        return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the headline kernel,
+# k_fact_hex<double,1,1,1,1>, on the 128^3 workload, from one ncu capture of
+#     ncu --set full --clock-control none -k regex:k_fact_hex -s 1 -c 1 -o fact_hex_fp64 \
+#         python bench.py --profile fp64 --steps 2 --warmup 1
+# (this run does not measure it; the bench line says so next to the value)
+C2_FP64_DRAM_BYTES_CAPTURED = 449_116_672
 
 
 class ClockSampler:
@@ -294,7 +291,7 @@ def run_ours(args, rank, world, local_rank):
     algo64 = algorithmic_bytes(cells, info.n_dofs, info.nnz, 8)
     algo32 = algorithmic_bytes(cells, info.n_dofs, info.nnz, 4)
     ach64 = algo64 / (ms_step * 1e-3) / 1e9
-    traffic = read_profile_traffic("k_fact_hex_fp64_c2_128")
+    traffic = C2_FP64_DRAM_BYTES_CAPTURED if args.n == 128 else None
     dp_ops = fp64_instructions(cfg)
     import ctypes
 
@@ -322,6 +319,8 @@ def run_ours(args, rank, world, local_rank):
                           "ms_per_step": totres / args.steps},
         "roofline": {"bound": "hbm", "achieved": ach64, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": ach64 / peaks["hbm_gbs"], "traffic": traffic,
+                     "traffic_source": "ncu capture of one launch of this kernel on this workload (dram read + write "
+                                       "bytes; a constant in bench.py, not measured by this run)",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": algo64,
                      "fp64_pipe": {"dp_instr_per_launch": dp_ops, "achieved_dp_instr_per_s": dp_ops / (ms_step * 1e-3),
@@ -389,7 +388,57 @@ def run_ours(args, rank, world, local_rank):
         except Exception as e:  # reported, never fatal
             out["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
+        out["targets"] = targets_summary(out)  # last key: survives a tail of the printed line
         print(json.dumps(out), flush=True)
+
+
+def targets_summary(out):
+    """The path's measurement targets in one compact object (values copied from the rest of the line)."""
+    def g(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r3(x):
+        return None if x is None else float(f"{x:.4g}")
+
+    t = {"c2_fp64_jacres_ms": r3(out["ms_per_step"]), "c2_mixed_jacres_ms": r3(g(out, "mixed", "ms_per_step")),
+         "c2_fp64_hbm_frac": r3(g(out, "roofline", "frac")),
+         "c2_fp64_pipe_frac": r3(g(out, "roofline", "fp64_pipe", "frac")),
+         "c2_e2e_cells_per_s": r3(g(out, "e2e", "value"))}
+    sol = out.get("solve") or {}
+    if sol:
+        t["c2_solve_mixed_speedup_e2e"] = {"gmg": r3(g(sol, "gmg", "mixed_speedup_e2e")),
+                                           "jacobi": r3(sol.get("mixed_speedup_e2e")),
+                                           "gmg_fp64_s": r3(g(sol, "gmg", "fp64", "seconds")),
+                                           "gmg_mixed_s": r3(g(sol, "gmg", "mixed", "seconds")),
+                                           "mixed_max_rel_diff_vs_fp64": r3(g(sol, "gmg", "mixed", "max_rel_diff_vs_fp64_jacobi")),
+                                           "mixed_rel_residual": r3(g(sol, "gmg", "mixed", "rel_residual_inf"))}
+    c3 = out.get("c3") or {}
+    if c3 and "error" not in c3:
+        t["c3"] = {"jac_fp32_plus_res_ms": r3(c3.get("jac_fp32_plus_res_ms_tensor_cores")),
+                   "jac_only_ms": r3(c3.get("jac_only_ms_tensor_cores")),
+                   "hbm_frac": r3(g(c3, "roofline", "hbm_frac")),
+                   "tensor_frac_issued": r3(g(c3, "roofline", "tensor_frac_issued")),
+                   "newton_mixed_gmg_s": r3(g(c3, "newton_mixed_gmg", "seconds")),
+                   "newton_rel_residual": r3(g(c3, "newton_mixed_gmg", "rel_residual_inf"))}
+    c4 = out.get("c4") or {}
+    if c4 and "error" not in c4:
+        t["c4"] = {"ms_per_batch": r3(c4.get("ms_per_batch")), "all_converged": c4.get("all_converged")}
+    c5 = out.get("c5") or {}
+    if c5 and "error" not in c5:
+        t["c5"] = {m: {"p50_ms": r3(g(c5, m, "p50_ms")), "p99_ms": r3(g(c5, m, "p99_ms")),
+                       "req_per_s": r3(g(c5, m, "req_per_s"))} for m in ("mixed", "fp64")}
+        t["c5"]["batch_req_per_s"] = r3(g(c5, "batch_mixed", "req_per_s"))
+        t["c5"]["at_80pct"] = {"p50_ms": r3(g(c5, "stream_at_80pct_batch", "p50_ms")),
+                               "p99_ms": r3(g(c5, "stream_at_80pct_batch", "p99_ms")),
+                               "p99_over_p50": r3(g(c5, "stream_at_80pct_batch", "p99_over_p50"))}
+    cb = out.get("cpu_baseline") or {}
+    if cb.get("value"):
+        t["cpu_baseline_cells_per_s"] = r3(cb["value"])
+    return t
 
 
 def _ev_time(fn, reps):
@@ -434,6 +483,21 @@ def bench_c3(args):
            "jac_fp32_cells_per_s_tensor_cores": info.n_cells / (t_jtc * 1e-3),
            "jac_only_ms_cuda_cores": t_j32_only, "jac_only_ms_tensor_cores": t_jtc_only,
            "contraction_tflops_tensor_cores": 2.0 * 27 * 27 * 108 * info.n_cells / (t_jtc_only * 1e-3) / 1e12}
+    # Roofline of the Jacobian-only pass on the tensor cores: algorithmic bytes = the FP32 CSR values written
+    # plus u read; algorithmic flops = 2*27*27*108 per cell (the B^T D B contraction); issued MMA flops =
+    # 3 products (3xTF32) * 2 * 112 (K padded) * 768 (27 rows padded to 28, plus 12) per cell.  The TF32
+    # dense rate is half the bf16 rate on this part: the denominator is half the measured bf16 GEMM rate.
+    peaks, peak_kind = read_peaks()
+    algo_bytes = info.nnz * 4 + info.n_dofs * 8
+    issued = 3 * 2.0 * 112 * 768 * info.n_cells
+    tf32_peak = 0.5 * peaks["bf16_tflops"] * 1e12
+    out["roofline"] = {"pass": "Jacobian only (coefficients, tensor-core element matrices, CSR rows)",
+                       "algorithmic_bytes": algo_bytes,
+                       "hbm_achieved_gbs": algo_bytes / (t_jtc_only * 1e-3) / 1e9,
+                       "hbm_frac": algo_bytes / (t_jtc_only * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                       "issued_tflops": issued / (t_jtc_only * 1e-3) / 1e12,
+                       "tensor_frac_issued": issued / (t_jtc_only * 1e-3) / tf32_peak,
+                       "peak_source": f"{peak_kind}: hbm_gbs; TF32 = bf16_tflops / 2"}
     del J32
     torch.cuda.empty_cache()
     # mixed Newton to 1e-10 with Jacobi BiCGStab (the reference's solver family) and with p-multigrid

@@ -299,6 +299,21 @@ int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J_vals_dev, const double
    an FMA-throughput kernel; the denominator of the FP64-pipe roofline.  No counterpart in the reference. */
 int mrg_measure_fma_rates(double* fp64_fma_per_s, double* fp32_fma_per_s, mrg_stream_t stream);
 
+/* ---- bounded device waits ---------------------------------------------------------------------
+   Every device-side wait of the library's kernels has a time limit: the tensor-core Q2 Jacobian's
+   mbarrier waits (default 2 s) and the staged SpMV's copy waits in mrg_spmv, the Krylov solvers and the
+   multigrid levels (default 1 s).  When a wait runs out, the kernel stops waiting, lets its own copies and
+   MMAs in flight land (bounded), frees the tensor memory it holds and exits, and the context stays usable.
+   The solvers report MRG_ETIMEOUT; the Q2 assembly, which does not synchronise, reports it on the next Q2
+   FP32 Jacobian call; mrg_spmv, which has no status word, leaves the rows of the timed-out tile unwritten.  No counterpart in the reference (its Kokkos kernels have no device waits).
+     limit_ns       the limit for this problem's kernels; 0 restores the defaults
+     withhold_copy  testing only: nonzero makes the first staged copy of those kernels never be issued, so
+                    that its wait runs out (exercises the time-out path without a fault); 0 for normal use
+   Waits for the handle's last stream and drops the problem's captured Krylov chunks and multigrid levels,
+   which are rebuilt on their next use with the new policy. */
+#define MRG_WAIT_LIMIT_MAX_NS 60000000000ull /* 60 s */
+int mrg_set_wait_policy(mrg_problem* p, uint64_t limit_ns, int32_t withhold_copy);
+
 /* ---- diagnostics ----------------------------------------------------------------------------- */
 int mrg_last_error(char* buf, size_t len);   /* copies the calling thread's last error message */
 const char* mrg_version(void);

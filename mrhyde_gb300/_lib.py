@@ -35,6 +35,7 @@ MRG_ASM_TENSOR_CORES = 4096
 MRG_ASM_CUDA_CORES = 8192
 MRG_ASM_NATIVE_FP64 = 16384
 MRG_NOALLOC_MAX_DOFS = 1 << 18
+MRG_WAIT_LIMIT_MAX_NS = 60_000_000_000
 
 
 class MeshDesc(C.Structure):
@@ -119,6 +120,7 @@ SIGNATURES = {
     "mrg_batch_autotune": (C.c_int, [_VP, _VP, _VP, C.POINTER(BatchOpts), _VP]),
     "mrg_batch_set_config": (C.c_int, [_VP, C.c_int32, C.c_int32]),
     "mrg_measure_fma_rates": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
+    "mrg_set_wait_policy": (C.c_int, [_VP, C.c_uint64, C.c_int32]),
     "mrg_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "mrg_version": (C.c_char_p, []),
 }

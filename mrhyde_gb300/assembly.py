@@ -152,6 +152,12 @@ class Problem:
         _require_cuda(kappa, "kappa", torch.float64, self.info.n_cells)
         L.check(L.lib().mrg_set_kappa(self._h, _ptr(kappa), _stream(stream)), "mrg_set_kappa")
 
+    def set_wait_policy(self, limit_ns: int = 0, withhold_copy: bool = False):
+        """Time limit of the device-side waits of this problem's kernels (0 = defaults); withhold_copy is
+        a testing switch that makes the first staged copy never be issued, so that its wait runs out."""
+        L.check(L.lib().mrg_set_wait_policy(self._h, int(limit_ns), 1 if withhold_copy else 0),
+                "mrg_set_wait_policy")
+
     def side_points(self, face: int) -> np.ndarray:
         """Coordinates [npts, 3] of the side quadrature points of `face` (0..2*dim-1 = x-, x+, y-, y+,
         z-, z+), ordered as mrg_set_face_bc expects its data."""

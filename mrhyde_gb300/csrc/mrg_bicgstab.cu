@@ -184,13 +184,7 @@ __global__ void __launch_bounds__(BT) k_b_update(int64_t nrows, BVec<VT, JT> V) 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 unsigned b_grid(const mrg_problem* p) {
-  static int nsm = 0;
-  if (nsm == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
-  }
-  const unsigned tiles = nblk(p->ndof, BT), cap = (unsigned)(16 * nsm);
+  const unsigned tiles = nblk(p->ndof, BT), cap = (unsigned)(16 * mrg_device_sms());
   return tiles < cap ? tiles : cap;
 }
 
@@ -217,6 +211,15 @@ struct BicgWork {
   const void* key[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   cudaStream_t gs[2] = {nullptr, nullptr};
 };
+
+void mrg_bicg_drop_graphs(mrg_problem* p) {
+  BicgWork* w = reinterpret_cast<BicgWork*>(p->bicg);
+  if (!w) return;
+  for (int k = 0; k < 2; ++k) {
+    if (w->g[k]) cudaGraphExecDestroy(w->g[k]);
+    w->g[k] = nullptr;
+  }
+}
 
 void mrg_bicg_free(mrg_problem* p) {
   BicgWork* w = reinterpret_cast<BicgWork*>(p->bicg);

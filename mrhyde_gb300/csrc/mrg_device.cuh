@@ -224,7 +224,7 @@ __host__ __device__ constexpr int wbuf_elems() { return WROWS * 27 + 2 * (16 / (
 template <typename JT>
 constexpr int wspmv_smem() { return (WST / 32) * 2 * wbuf_elems<JT>() * (int)sizeof(JT); }
 
-constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on one tile's copy
+constexpr unsigned long long WAIT_NS = 1000000000ull;  // default bound on one tile's copy: 1 s
 
 __device__ __forceinline__ bool wbar_try(uint32_t mbar, uint32_t parity) {
   uint32_t ok;
@@ -242,13 +242,13 @@ __device__ __forceinline__ uint64_t wtimer() {
   return t;
 }
 
-// bounded wait by every lane of the warp; the result is warp-uniform
-__device__ __forceinline__ bool wbar_wait(uint32_t mbar, uint32_t parity) {
+// bounded wait by every lane of the warp (limit in ns); the result is warp-uniform
+__device__ __forceinline__ bool wbar_wait(uint32_t mbar, uint32_t parity, unsigned long long limit) {
   int ok = 1;
   if (!wbar_try(mbar, parity)) {
     const uint64_t t0 = wtimer();
     while (!wbar_try(mbar, parity))
-      if (wtimer() - t0 > WAIT_NS) { ok = 0; break; }
+      if (wtimer() - t0 > limit) { ok = 0; break; }
   }
   return __all_sync(0xffffffffu, ok) != 0;
 }
@@ -289,7 +289,8 @@ __device__ __forceinline__ uintptr_t wtile_issue(const Grid& g, int64_t nrows, c
   if (lane < nhead) *reinterpret_cast<JT*>(sb + (lo - base) + lane * E) = __ldcs(reinterpret_cast<const JT*>(lo) + lane);
   if (lane >= 8 && lane - 8 < ntail)
     *reinterpret_cast<JT*>(sb + (t0 - base) + (lane - 8) * E) = __ldcs(reinterpret_cast<const JT*>(t0) + (lane - 8));
-  if (lane == 0) {
+  // g.withhold (testing): the copy of tile 0 is never issued, so the wait for it runs out
+  if (lane == 0 && !(g.withhold && tile == 0)) {
     const uint32_t bytes = (uint32_t)(b1 - b0);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
     if (bytes)
@@ -319,6 +320,7 @@ __device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, c
   __syncwarp();
   const int64_t ntiles = (nrows + WROWS - 1) / WROWS;
   const int64_t W = (int64_t)gridDim.x * (WST / 32);
+  const unsigned long long limit = g.wait_ns ? g.wait_ns : WAIT_NS;
   int64_t tile = (int64_t)blockIdx.x * (WST / 32) + w;
   // buffer b of the current tile; the other buffer receives the next tile
   uintptr_t base0 = 0, base1 = 0;
@@ -336,7 +338,7 @@ __device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, c
       if (b == 0) { base1 = wtile_issue<JT>(g, nrows, J, nxt, buf1, mb1, lane, Rn); armed1 = true; }
       else        { base0 = wtile_issue<JT>(g, nrows, J, nxt, buf0, mb0, lane, Rn); armed0 = true; }
     }
-    const bool got = (b == 0) ? wbar_wait(mb0, ph0) : wbar_wait(mb1, ph1);
+    const bool got = (b == 0) ? wbar_wait(mb0, ph0, limit) : wbar_wait(mb1, ph1, limit);
     if (!got) { ok = false; break; }
     if (b == 0) { ph0 ^= 1u; armed0 = false; } else { ph1 ^= 1u; armed1 = false; }
     __syncwarp();
@@ -351,8 +353,8 @@ __device__ __forceinline__ bool warp_staged_rows(const Grid& g, int64_t nrows, c
     b ^= 1;
   }
   if (!ok) {  // let copies still in flight land before the CTA exits (bounded)
-    if (armed0) wbar_wait(mb0, ph0);
-    if (armed1) wbar_wait(mb1, ph1);
+    if (armed0) wbar_wait(mb0, ph0, limit);
+    if (armed1) wbar_wait(mb1, ph1, limit);
   }
   return ok;
 }

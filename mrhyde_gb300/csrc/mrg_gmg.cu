@@ -982,15 +982,7 @@ __global__ void __launch_bounds__(NT) k_bg_update(int64_t n, BgVec<T> V) {
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-int num_sms() {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
-  }
-  return nsm;
-}
+int num_sms() { return mrg_device_sms(); }
 
 unsigned grid_for(int64_t n, int per_sm) {
   const unsigned need = nblk(n, NT), cap = (unsigned)(per_sm * num_sms());
@@ -1525,6 +1517,15 @@ int gmg_bicgstab(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double
 
 int mrg_gmg_kind(const mrg_problem* p) {
   return p->gmg ? reinterpret_cast<const GmgData*>(p->gmg)->kind : MRG_PREC_JACOBI;
+}
+
+void mrg_gmg_drop_hierarchy(mrg_problem* p) {
+  GmgData* G = reinterpret_cast<GmgData*>(p->gmg);
+  if (!G) return;
+  free_hier(G->h64, p->stream);
+  free_hier(G->h32, p->stream);
+  G->h64 = nullptr;
+  G->h32 = nullptr;
 }
 
 void mrg_gmg_free(mrg_problem* p) {

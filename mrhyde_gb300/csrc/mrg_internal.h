@@ -22,6 +22,9 @@ int mrg_cuda_check(cudaError_t e, const char* what);
 void* mrg_pinned_slot();
 void mrg_pinned_release(void* p);
 
+// Number of SMs of the current device, cached per device ordinal (any host thread).
+int mrg_device_sms();
+
 #define MRG_CUDA(call)                                          \
   do {                                                          \
     cudaError_t e__ = (call);                                   \
@@ -46,6 +49,11 @@ struct Grid {
   uint32_t faces;  // Dirichlet face mask
   int64_t T[3];    // per-axis totals of the coupling counts
   const int64_t* P[3];  // device per-axis prefix tables, length nn[k]+1
+  // bounded device waits (mrg_set_wait_policy): limit in ns (0 = the kernel's default) and the testing
+  // switch that withholds the first staged copy so that its wait runs out
+  unsigned long long wait_ns;
+  int withhold;
+  int reserved;
 };
 
 // Coupled node range along one axis for node index i (host + device).
@@ -156,6 +164,9 @@ int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, 
                      mrg_solve_stats* st, bool reuse_setup, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);
+void mrg_solver_drop_graphs(mrg_problem* p);  // captured PCG chunks (recaptured on next use)
+void mrg_bicg_drop_graphs(mrg_problem* p);    // captured BiCGStab chunks
+void mrg_gmg_drop_hierarchy(mrg_problem* p);  // multigrid levels and graphs (rebuilt on next use)
 int mrg_residual_from(mrg_problem* p, const double* b, double* res, cudaStream_t s);  // res = b - res
 // BiCGStab (mrg_bicgstab.cu)
 void mrg_bicg_free(mrg_problem* p);

@@ -1,6 +1,7 @@
 // Problem lifetime, structure queries, coefficients, Dirichlet data and the assembly dispatcher
 // of the C ABI declared in include/mrhyde_gb300.h.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -51,6 +52,28 @@ void mrg_pinned_release(void* p) {
   if (!p) return;
   std::lock_guard<std::mutex> lk(g_pin_mu);
   g_pin_free.push_back(p);
+}
+
+// ------------------------------------------------------------------------------------------------
+// SM count of the current device, looked up once per device ordinal (safe from any host thread)
+// ------------------------------------------------------------------------------------------------
+namespace {
+constexpr int SM_CACHE = 256;
+std::atomic<int> g_sm_count[SM_CACHE];
+}  // namespace
+
+int mrg_device_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  if (dev >= 0 && dev < SM_CACHE) {
+    const int c = g_sm_count[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int nsm = 0;
+  if (dev < 0 || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+    return 148;  // conservative grid sizing when the query fails; not cached
+  if (dev < SM_CACHE) g_sm_count[dev].store(nsm, std::memory_order_relaxed);
+  return nsm;
 }
 
 extern "C" int mrg_last_error(char* buf, size_t len) {
@@ -499,6 +522,21 @@ extern "C" int mrg_problem_create_on_stream(const mrg_mesh_desc* m, const mrg_ph
 extern "C" int mrg_problem_destroy(mrg_problem* p) {
   if (!p) return MRG_EINVAL;
   free_problem(p);
+  return MRG_OK;
+}
+
+extern "C" int mrg_set_wait_policy(mrg_problem* p, uint64_t limit_ns, int32_t withhold_copy) {
+  if (!p) return mrg_fail(MRG_EINVAL, "mrg_set_wait_policy: null problem");
+  if (limit_ns > MRG_WAIT_LIMIT_MAX_NS)
+    return mrg_fail(MRG_EINVAL, "mrg_set_wait_policy: limit above MRG_WAIT_LIMIT_MAX_NS");
+  // captured graphs and multigrid levels hold copies of the grid description: let the work in flight
+  // finish, then drop them so that the next solve records the new policy
+  MRG_CUDA(cudaStreamSynchronize(p->last_stream));
+  p->g.wait_ns = (unsigned long long)limit_ns;
+  p->g.withhold = withhold_copy ? 1 : 0;
+  mrg_solver_drop_graphs(p);
+  mrg_bicg_drop_graphs(p);
+  mrg_gmg_drop_hierarchy(p);
   return MRG_OK;
 }
 

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(ST) k_spmv(Grid g, int64_t nrows, const JT* __
 }
 
 // ---- FP64 PCG kernels ---------------------------------------------------------------------------
-// All PCG kernels are grid-stride loops over a fixed grid of at most 8 CTAs per SM, so that each
+// All PCG kernels are grid-stride loops over a fixed grid of at most 16 CTAs per SM, so that each
 // deterministic reduction has at most a few thousand per-CTA partials and counter increments.
 struct PcgVec64 {
   double *x, *r, *z, *p, *q, *minv, *parts;
@@ -146,7 +146,10 @@ __global__ void __launch_bounds__(ST) k_pcg64_spmv(Grid g, int64_t nrows, PcgVec
       PcgScal* s = V.s;
       s->pq = t[0];
       s->alpha = s->rho / t[0];
-      if (!(t[0] > 0.0) || !isfinite(s->alpha)) { s->status = MRG_ENUMERIC; s->done = 1; }
+      if (!(t[0] > 0.0) || !isfinite(s->alpha)) {
+        if (s->status == MRG_OK) s->status = MRG_ENUMERIC;
+        s->done = 1;
+      }
     }
   }
 }
@@ -197,7 +200,10 @@ __global__ void __launch_bounds__(ST) k_pcg64_update(int64_t nrows, PcgVec64 V) 
       s->beta = s->rho / s->rho_old;
       s->iter += 1;
       if (!(s->rnorm / s->r0 > s->tol) || s->iter >= s->maxiter) s->done = 1;
-      if (!isfinite(s->rnorm)) { s->done = 1; s->status = MRG_ENUMERIC; }
+      if (!isfinite(s->rnorm)) {
+        s->done = 1;
+        if (s->status == MRG_OK) s->status = MRG_ENUMERIC;
+      }
     }
   }
 }
@@ -306,7 +312,10 @@ __global__ void __launch_bounds__(ST) k_pcg32_spmv(Grid g, int64_t nrows, PcgVec
       PcgScal* s = V.s;
       s->pq = t[0];
       s->alpha = s->rho / t[0];
-      if (!(t[0] > 0.0) || !isfinite(s->alpha)) { s->status = MRG_ENUMERIC; s->done = 1; }
+      if (!(t[0] > 0.0) || !isfinite(s->alpha)) {
+        if (s->status == MRG_OK) s->status = MRG_ENUMERIC;
+        s->done = 1;
+      }
     }
   }
 }
@@ -356,7 +365,10 @@ __global__ void __launch_bounds__(ST) k_pcg32_update(int64_t nrows, PcgVec32 V) 
       s->beta = s->rho / s->rho_old;
       s->iter += 1;
       if (!(s->rnorm / s->r0 > s->tol) || s->iter >= s->maxiter) s->done = 1;
-      if (!isfinite(s->rnorm)) { s->done = 1; s->status = MRG_ENUMERIC; }
+      if (!isfinite(s->rnorm)) {
+        s->done = 1;
+        if (s->status == MRG_OK) s->status = MRG_ENUMERIC;
+      }
     }
   }
 }
@@ -396,16 +408,22 @@ __global__ void __launch_bounds__(ST) k_norminf(int64_t n, const double* __restr
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-// grid of the PCG kernels: one CTA per 128-row tile, at most 8 CTAs per SM
-inline unsigned pcg_grid(const mrg_problem* p, int per_sm = 16) {
-  static int nsm = 0;
-  if (nsm == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 148;
+// host message for a failed PCG, chosen from the device status word
+inline std::string pcg_status_text(const char* who, int status) {
+  switch (status) {
+    case MRG_ETIMEOUT:
+      return std::string(who) + ": a CSR staging copy of the SpMV did not complete within its time bound";
+    case MRG_ENUMERIC:
+      return std::string(who) + ": non-positive or non-finite curvature (matrix not SPD?) or non-finite residual";
+    default:
+      return std::string(who) + ": failed with status " + std::to_string(status);
   }
+}
+
+// grid of the PCG kernels: one CTA per 128-row tile, at most per_sm CTAs per SM of the current device
+inline unsigned pcg_grid(const mrg_problem* p, int per_sm = 16) {
   const unsigned tiles = nblk(p->ndof, ST);
-  const unsigned cap = (unsigned)(per_sm * nsm);
+  const unsigned cap = (unsigned)(per_sm * mrg_device_sms());
   return tiles < cap ? tiles : cap;
 }
 
@@ -450,6 +468,14 @@ void mrg_solver_free(mrg_problem* p) {
   mrg_pinned_release(w->h_s);
   delete w;
   p->work = nullptr;
+}
+
+void mrg_solver_drop_graphs(mrg_problem* p) {
+  SolverWork* w = p->work;
+  if (!w) return;
+  if (w->g64) cudaGraphExecDestroy(w->g64);
+  if (w->g32) cudaGraphExecDestroy(w->g32);
+  w->g64 = w->g32 = nullptr;
 }
 
 static int ensure_work(mrg_problem* p, bool need64, bool need32, cudaStream_t st) {
@@ -586,7 +612,7 @@ static int pcg64(mrg_problem* p, const double* J, const double* b, double* x, do
     st->abs_residual = h->rnorm;
     st->status = h->status;
   }
-  if (h->status != MRG_OK) return mrg_fail(h->status, "PCG: non-positive or non-finite curvature (matrix not SPD?)");
+  if (h->status != MRG_OK) return mrg_fail(h->status, pcg_status_text("PCG", h->status));
   if (h->r0 > 0 && h->rnorm / h->r0 > rtol) {
     if (st) st->status = MRG_ENOCONV;
     return mrg_fail(MRG_ENOCONV, "PCG: maximum iterations reached before the tolerance");
@@ -620,7 +646,7 @@ static int pcg32(mrg_problem* p, const float* J, const double* b, double rtol, i
     st->abs_residual = h->rnorm;
     st->status = h->status;
   }
-  if (h->status != MRG_OK) return mrg_fail(h->status, "PCG (FP32): non-positive or non-finite curvature");
+  if (h->status != MRG_OK) return mrg_fail(h->status, pcg_status_text("PCG (FP32)", h->status));
   return MRG_OK;
 }
 
@@ -913,7 +939,7 @@ extern "C" int mrg_solve_pcg_noalloc(mrg_problem* p, const double* J, const doub
     st->abs_residual = h.rnorm;
     st->status = h.status;
   }
-  if (h.status != MRG_OK) return mrg_fail(h.status, "PCG (no-alloc): non-positive or non-finite curvature");
+  if (h.status != MRG_OK) return mrg_fail(h.status, pcg_status_text("PCG (no-alloc)", h.status));
   if (h.r0 > 0 && h.rnorm / h.r0 > rtol) {
     if (st) st->status = MRG_ENOCONV;
     return mrg_fail(MRG_ENOCONV, "PCG (no-alloc): maximum iterations reached before the tolerance");

@@ -79,7 +79,7 @@ static_assert(SMEM_BYTES <= 232448, "shared memory budget");
 // kind::tf32 instruction descriptor: D = F32, A = B = TF32, both K-major, N = 256, M = 128
 constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NCH >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 
-constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s: far above any legitimate wait
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // default wait bound, 2 s: far above any legitimate wait
 
 __device__ __forceinline__ uint64_t gtimer() {
   uint64_t t;
@@ -97,16 +97,17 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase.  Returns false (and raises the CTA abort flag) on time-out, or
-// false when another role has already aborted.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, volatile int* abort_flag) {
+// Bounded wait (limit in ns) on an mbarrier phase.  Returns false (and raises the CTA abort flag) on
+// time-out, or false when another role has already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, volatile int* abort_flag,
+                                          unsigned long long limit) {
   if (mbar_try(mbar, parity)) return true;
   const uint64_t t0 = gtimer();
   for (uint32_t i = 1;; ++i) {
     if (mbar_try(mbar, parity)) return true;
     if ((i & 63u) == 0) {
       if (*abort_flag) return false;
-      if (gtimer() - t0 > WAIT_NS) {
+      if (gtimer() - t0 > limit) {
         *abort_flag = 1;
         return false;
       }
@@ -167,7 +168,7 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 
 __global__ void __launch_bounds__(THREADS, 1)
     k_q2_elem_tc(const float* __restrict__ wimg, const float* __restrict__ himg, const __grid_constant__ CUtensorMap mE,
-                 int ntiles, int ksteps, int* __restrict__ err) {
+                 int ntiles, int ksteps, int* __restrict__ err, unsigned long long wait_ns, int withhold) {
   extern __shared__ unsigned char sm_raw[];
   const uint32_t raw = (uint32_t)__cvta_generic_to_shared(sm_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const int kchunks = 2 * ksteps;  // 16-byte K chunks of W per tile
+  const unsigned long long lim = wait_ns ? wait_ns : WAIT_NS;
 
   if (warp == 0) {
     // ------------------------------ TMA producer ------------------------------
@@ -215,17 +217,21 @@ __global__ void __launch_bounds__(THREADS, 1)
       int b_armed[NBS];
       for (int s = 0; s < NBS; ++s) b_armed[s] = -1;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++ta) {
-        if (!mbar_wait(bar(BAR_A_EMPTY), (ta & 1u) ^ 1u, abort_flag)) { ok = false; break; }
-        const uint32_t abytes = (uint32_t)(kchunks * TM * 16);
-        mbar_expect_tx(bar(BAR_A_FULL), 2u * abytes);
-        a_armed = (int)(ta & 1u);
-        const float* wt = wimg + (size_t)tile * W_TILE_FLOATS;
-        bulk_load(sAh, wt, abytes, bar(BAR_A_FULL));
-        bulk_load(sAl, wt + TM * KH, abytes, bar(BAR_A_FULL));
+        if (!mbar_wait(bar(BAR_A_EMPTY), (ta & 1u) ^ 1u, abort_flag, lim)) { ok = false; break; }
+        // withhold (testing): the W copy of tile 0 is never issued, so the MMA thread's wait for it runs
+        // out and the abort path is taken with no copy in flight on that barrier
+        if (!(withhold && tile == 0)) {
+          const uint32_t abytes = (uint32_t)(kchunks * TM * 16);
+          mbar_expect_tx(bar(BAR_A_FULL), 2u * abytes);
+          a_armed = (int)(ta & 1u);
+          const float* wt = wimg + (size_t)tile * W_TILE_FLOATS;
+          bulk_load(sAh, wt, abytes, bar(BAR_A_FULL));
+          bulk_load(sAl, wt + TM * KH, abytes, bar(BAR_A_FULL));
+        }
         for (int n = 0; n < NNCH && ok; ++n)
           for (int ks = 0; ks < ksteps; ++ks, ++bit) {
             const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
-            if (!mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag)) { ok = false; break; }
+            if (!mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag, lim)) { ok = false; break; }
             mbar_expect_tx(bar(BAR_B_FULL + st), (uint32_t)B_STAGE);
             b_armed[st] = (int)ph;
             bulk_load(sB + st * B_STAGE, himg + (size_t)(n * KSTEPS_MAX + ks) * H_STAGE_FLOATS, (uint32_t)B_STAGE,
@@ -236,7 +242,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         // tail: wait until the MMA thread has released every stage, so that no arrive lands after exit
         for (int s = 0; s < NBS && ok; ++s, ++bit) {
           const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
-          if (b_armed[st] >= 0 && !mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag)) ok = false;
+          if (b_armed[st] >= 0 && !mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag, lim)) ok = false;
         }
       }
       if (!ok) {
@@ -253,16 +259,16 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true, issued = false;
       uint32_t bit = 0, acc = 0, ta = 0;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++ta) {
-        if (!mbar_wait(bar(BAR_A_FULL), ta & 1u, abort_flag)) { ok = false; break; }
+        if (!mbar_wait(bar(BAR_A_FULL), ta & 1u, abort_flag, lim)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         for (int n = 0; n < NNCH && ok; ++n, ++acc) {
           const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
-          if (!mbar_wait(bar(BAR_T_EMPTY + buf), aph ^ 1u, abort_flag)) { ok = false; break; }
+          if (!mbar_wait(bar(BAR_T_EMPTY + buf), aph ^ 1u, abort_flag, lim)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
           const uint32_t d = tmem + buf * NCH;
           for (int ks = 0; ks < ksteps; ++ks, ++bit) {
             const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
-            if (!mbar_wait(bar(BAR_B_FULL + st), ph, abort_flag)) { ok = false; break; }
+            if (!mbar_wait(bar(BAR_B_FULL + st), ph, abort_flag, lim)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t bh = sB + st * B_STAGE, bl = bh + B_PLANE;
             const uint32_t koff = (uint32_t)ks * 2u * (TM * 16);
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int n = 0; n < NNCH; ++n, ++acc) {
         const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
         int good = 1;
-        if (lane == 0) good = mbar_wait(bar(BAR_T_FULL + buf), aph, abort_flag) ? 1 : 0;
+        if (lane == 0) good = mbar_wait(bar(BAR_T_FULL + buf), aph, abort_flag, lim) ? 1 : 0;
         good = __shfl_sync(0xffffffffu, good, 0);
         if (!good) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -596,7 +602,8 @@ int mrg_q2tc_launch(const mrg_problem* p, Q2Tc* T, float* J, bool ovw, int* err,
   MRG_CUDA(cudaGetDevice(&dev));
   MRG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const int grid = T->ntiles < nsm ? T->ntiles : nsm;
-  k_q2_elem_tc<<<grid, THREADS, SMEM_BYTES, s>>>(T->d_w, T->d_h, T->mE, T->ntiles, T->ksteps, err);
+  k_q2_elem_tc<<<grid, THREADS, SMEM_BYTES, s>>>(T->d_w, T->d_h, T->mE, T->ntiles, T->ksteps, err, p->g.wait_ns,
+                                                 p->g.withhold);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return mrg_cuda_check(e, "tensor-core element kernel launch");
   if ((int64_t)p->g.nc[0] * p->g.nc[1] * NE * 2 >= ((int64_t)1 << 31))

@@ -7,7 +7,8 @@ a run stopping at the first failure has already run every other test; it also pa
 fresh process.
 
 Checked through the C ABI: two calls in a row agree with mrg_solve_pcg (same tolerance as the other
-PCG tests: 1e-9 of the solution's max norm), and a problem above the fixed limit is rejected.
+PCG tests: 1e-9 of the solution's max norm), a call after a warm-up call leaves the device's free
+memory and torch's allocator counters unchanged, and a problem above the fixed limit is rejected.
 """
 import ctypes as C
 
@@ -47,6 +48,40 @@ def test_noalloc_pcg_matches_allocating_pcg_twice(cuda):
         assert st.rel_residual <= 1e-10
         assert st.iterations == ref.iterations
         np.testing.assert_allclose(x.cpu().numpy(), xr, rtol=0, atol=1e-9 * np.abs(xr).max())
+
+
+@pytest.mark.gpu
+def test_noalloc_pcg_allocates_nothing(cuda):
+    """After a warm-up call (which loads the kernels and looks up the scratch array's address), a call
+    changes neither the device's free memory (cudaMemGetInfo, which sees every allocation on the device,
+    library or torch) nor torch's allocation counters."""
+    from mrhyde_gb300 import AssemblyManager, Problem
+    from mrhyde_gb300 import _lib as L
+
+    rng = np.random.default_rng(13)
+    n = (30, 30, 30)
+    P = Problem(dim=3, order=1, n=n, kappa=np.exp(0.5 * rng.standard_normal(int(np.prod(n)))),
+                source=("const", 1.0, 0.0), dirichlet_faces=3)
+    A = AssemblyManager(P)
+    u, r, J = P.new_vector(), P.new_vector(), P.new_matrix_values()
+    A.assembleJacRes(u, r, J, overwrite=True)
+    x0, x1 = P.new_vector(), P.new_vector()
+    rc, _ = _solve_noalloc(L, P, J, r, x0, 1e-10, 5000)  # warm-up
+    assert rc == L.MRG_OK, L.last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    rc, st = _solve_noalloc(L, P, J, r, x1, 1e-10, 5000)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert rc == L.MRG_OK, L.last_error()
+    assert st.rel_residual <= 1e-10
+    assert free1 == free0, (free0, free1)
+    for key in ("allocation.all.allocated", "segment.all.allocated", "allocated_bytes.all.current",
+                "reserved_bytes.all.current"):
+        assert stats1.get(key, 0) == stats0.get(key, 0), key
+    assert torch.equal(x0, x1)
 
 
 @pytest.mark.gpu
