@@ -374,7 +374,7 @@ def run_ours(args, rank, world, local_rank):
         out["solve"] = sol
 
     if not args.no_extras:
-        for name, fn in (("c3", bench_c3), ("c4", bench_c4),
+        for name, fn in (("general", bench_general), ("c3", bench_c3), ("c4", bench_c4),
                          ("c5", lambda a: bench_c5(a, rank, world, dist))):
             try:
                 out[name] = fn(args)
@@ -424,6 +424,12 @@ def targets_summary(out):
                    "tensor_frac_issued": r3(g(c3, "roofline", "tensor_frac_issued")),
                    "newton_mixed_gmg_s": r3(g(c3, "newton_mixed_gmg", "seconds")),
                    "newton_rel_residual": r3(g(c3, "newton_mixed_gmg", "rel_residual_inf"))}
+    gen = out.get("general") or {}
+    if gen and "error" not in gen:
+        t["general_noaffine"] = {"fp64_jacres_ms": r3(gen.get("fp64_jacres_ms")),
+                                 "mixed_jacres_ms": r3(gen.get("mixed_jacres_ms")),
+                                 "residual_ms": r3(gen.get("residual_ms")),
+                                 "hbm_frac_fp64": r3(gen.get("hbm_frac_fp64"))}
     c4 = out.get("c4") or {}
     if c4 and "error" not in c4:
         t["c4"] = {"ms_per_batch": r3(c4.get("ms_per_batch")), "all_converged": c4.get("all_converged")}
@@ -517,6 +523,39 @@ def bench_c3(args):
                     "dof_per_s": info.n_dofs / dt}
     SolverManager(P, preconditioner="jacobi")
     return out
+
+
+def bench_general(args):
+    """C2's coefficients, source and boundary data on non-affine hexahedra (interior vertices moved by up to
+    0.2 h): the general per-cell path (geometry per cell, forward-AD tangents in registers, coloured
+    scatter) -- what a mesh that is not a uniform box gets."""
+    import torch
+
+    from mrhyde_gb300 import AssemblyManager, Problem
+    from mrhyde_gb300.workloads import c2_general
+
+    n = args.general_n
+    P = Problem(**c2_general(seed=2, n=n))
+    info = P.info
+    A = AssemblyManager(P)
+    u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, info.n_dofs), device="cuda")
+    r = P.new_vector()
+    J64 = P.new_matrix_values(fp32=False)
+    t64 = _ev_time(lambda: A.assembleJacRes(u, r, J64, overwrite=True), 3)
+    del J64
+    J32 = P.new_matrix_values(fp32=True)
+    t32 = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True), 3)
+    del J32
+    tres = _ev_time(lambda: A.assembleRes(u, r, overwrite=True), 3)
+    torch.cuda.empty_cache()
+    peaks, peak_kind = read_peaks()
+    algo = algorithmic_bytes(info.n_cells, info.n_dofs, info.nnz, 8)
+    return {"workload": f"{n}^3 Q1 hex, interior vertices perturbed by up to 0.2 h (non-affine), C2 coefficients",
+            "path": info.path, "cells": info.n_cells, "dofs": info.n_dofs, "nnz": info.nnz,
+            "fp64_jacres_ms": t64, "fp64_cells_per_s": info.n_cells / (t64 * 1e-3),
+            "mixed_jacres_ms": t32, "mixed_cells_per_s": info.n_cells / (t32 * 1e-3),
+            "residual_ms": tres, "residual_cells_per_s": info.n_cells / (tres * 1e-3),
+            "hbm_frac_fp64": algo / (t64 * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes": algo}
 
 
 def bench_c4(args):
@@ -675,6 +714,18 @@ def run_profile(args, local_rank):
         torch.cuda.synchronize()
         print(json.dumps({"profile": "c4", "steps": args.steps, "ok": True}))
         return
+    if args.profile in ("cell64", "cell32"):  # the per-cell path on non-affine hexahedra (C2 coefficients)
+        from mrhyde_gb300.workloads import c2_general
+
+        P = Problem(**c2_general(seed=2, n=args.general_n))
+        A = AssemblyManager(P)
+        u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, P.info.n_dofs), device="cuda")
+        r, J = P.new_vector(), P.new_matrix_values(fp32=args.profile == "cell32")
+        for _ in range(args.warmup + args.steps):
+            A.assembleJacRes(u, r, J, fp32_jacobian=args.profile == "cell32", overwrite=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.profile, "n": args.general_n, "steps": args.steps, "ok": True}))
+        return
     if args.profile in ("q2tc", "q2cc"):
         from mrhyde_gb300.workloads import c3
 
@@ -726,9 +777,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the C3/C4/C5 measurements")
     ap.add_argument("--c3-n", type=int, default=64)
+    ap.add_argument("--general-n", type=int, default=128, help="cells per axis of the non-affine mesh leg")
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4"],
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4",
+                             "cell64", "cell32"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

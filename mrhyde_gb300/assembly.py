@@ -108,6 +108,9 @@ class Problem:
         self._h = h
         self.dim, self.order = dim, order
         self.n = tuple(int(v) for v in n[:dim])
+        self.lo = tuple(float(lo[k]) if k < len(lo) else 0.0 for k in range(dim))
+        self.hi = tuple(float(hi[k]) if k < len(hi) else 1.0 for k in range(dim))
+        self.vertex_coords = keep[0] if vertex_coords is not None else None  # host copy, x fastest
         info = L.ProblemInfo()
         L.check(lib.mrg_problem_get_info(self._h, C.byref(info)), "mrg_problem_get_info")
         self.info = ProblemInfo(info.n_dofs, info.n_cells, info.nnz, info.n_fixed, info.nodes_per_cell,
