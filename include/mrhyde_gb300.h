@@ -112,8 +112,13 @@ typedef struct mrg_problem_info {
 enum {
   MRG_PATH_FACTORED = 1,   /* identical affine cells: K_e = kappa_c * K_ref, row-gather assembly */
   MRG_PATH_CELL = 2,       /* per-cell geometry + forward-AD tangents in registers, colored scatter */
-  MRG_PATH_TENSOR = 3      /* identical affine hexahedra, Q2 or nonlinear Q1: sum-factorised FP64 residual,
+  MRG_PATH_TENSOR = 3,     /* identical affine hexahedra, Q2 or nonlinear Q1: sum-factorised FP64 residual,
                               row-gather Jacobian (each (row, cell) pair one row of a constant-operand GEMM) */
+  MRG_PATH_STORED = 4      /* thermal Q1 hexahedra of general geometry: each cell's kappa-free stiffness (FP64
+                              and FP32) and the node loads computed once at creation (the reference's stored
+                              per-cell basis data, "storage proportion" 1.0; 432 bytes a cell and 8 a node),
+                              row-gather assembly.  MRG_ASM_FORCE_CELL or MRG_ASM_ATOMIC select the per-cell
+                              AD kernels instead */
 };
 
 /* mrg_assemble flags */
@@ -124,7 +129,7 @@ enum {
   MRG_ASM_OVERWRITE = 8u,      /* fused J.setAllToScalar(0), r.putScalar(0)      */
   MRG_ASM_FIX_ZERO_ROWS = 16u, /* "fix zero rows" (jacres:609-628)               */
   MRG_ASM_FORCE_CELL = 256u,   /* force the per-cell AD path (testing)           */
-  MRG_ASM_ATOMIC = 512u,       /* per-cell path: atomic scatter instead of 8-colour scatter */
+  MRG_ASM_ATOMIC = 512u,       /* per-cell AD path with atomic scatter instead of the 8-colour scatter */
   MRG_ASM_ADJOINT = 1024u,     /* not supported -> MRG_ENOTSUP                   */
   MRG_ASM_SENS = 2048u,        /* not supported -> MRG_ENOTSUP                   */
   MRG_ASM_TENSOR_CORES = 4096u,/* Q2 FP32 Jacobian: element contractions on tcgen05 tensor cores (3xTF32);

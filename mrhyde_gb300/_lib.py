@@ -20,7 +20,7 @@ MRG_DBC_CONST, MRG_DBC_NODE = 0, 1
 MRG_FACE_XLO, MRG_FACE_XHI, MRG_FACE_YLO, MRG_FACE_YHI, MRG_FACE_ZLO, MRG_FACE_ZHI = 1, 2, 4, 8, 16, 32
 MRG_FACE_ALL = 63
 MRG_BC_NONE, MRG_BC_NEUMANN, MRG_BC_WEAK_DIRICHLET = 0, 1, 2
-MRG_PATH_FACTORED, MRG_PATH_CELL, MRG_PATH_TENSOR = 1, 2, 3
+MRG_PATH_FACTORED, MRG_PATH_CELL, MRG_PATH_TENSOR, MRG_PATH_STORED = 1, 2, 3, 4
 
 MRG_ASM_RES = 1
 MRG_ASM_JAC = 2

@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "mrg_device.cuh"
 #include "mrg_fixmul.cuh"
 #include "mrg_internal.h"
 
@@ -58,47 +59,8 @@ __device__ __forceinline__ bool nonfinite(double v) {
   return ((unsigned)__double2hiint(v) & 0x7ff00000u) == 0x7ff00000u;
 }
 
-__device__ __forceinline__ int64_t row_ptr_of(const Grid& g, int64_t n, int64_t nrows) {
-  if (n >= nrows) return g.T[0] * g.T[1] * g.T[2];
-  int ix, iy, iz;
-  decompose(g, n, ix, iy, iz);
-  int lo, cx, cy, cz;
-  axis_range(ix, g.nn[0], g.p, lo, cx);
-  axis_range(iy, g.nn[1], g.p, lo, cy);
-  if (g.dim == 3) axis_range(iz, g.nn[2], g.p, lo, cz); else cz = 1;
-  return g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
-}
-
-// Copy (or add) a contiguous segment from shared memory to global memory.  src[k] <-> dst[k]; both
-// pointers have the same address phase modulo 16 bytes, so the body uses aligned 16-byte accesses.
-template <typename T, bool ADD>
-__device__ __forceinline__ void seg_store(T* __restrict__ dst, const T* __restrict__ src, int64_t len) {
-  constexpr int V = 16 / sizeof(T);
-  int head = (int)(((16 - ((uintptr_t)dst & 15)) & 15) / sizeof(T));
-  if (head > len) head = (int)len;
-  for (int k = threadIdx.x; k < head; k += blockDim.x) {
-    if (ADD) dst[k] += src[k]; else dst[k] = src[k];
-  }
-  int64_t body = (len - head) / V;
-  if constexpr (sizeof(T) == 8) {
-    const double2* s2 = reinterpret_cast<const double2*>(src + head);
-    double2* d2 = reinterpret_cast<double2*>(dst + head);
-    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) {
-      double2 x = s2[v];
-      if (ADD) { double2 y = d2[v]; x.x += y.x; x.y += y.y; d2[v] = x; } else __stcs(d2 + v, x);
-    }
-  } else {
-    const float4* s4 = reinterpret_cast<const float4*>(src + head);
-    float4* d4 = reinterpret_cast<float4*>(dst + head);
-    for (int64_t v = threadIdx.x; v < body; v += blockDim.x) {
-      float4 x = s4[v];
-      if (ADD) { float4 y = d4[v]; x.x += y.x; x.y += y.y; x.z += y.z; x.w += y.w; d4[v] = x; } else __stcs(d4 + v, x);
-    }
-  }
-  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) {
-    if (ADD) dst[k] += src[k]; else dst[k] = src[k];
-  }
-}
+using mrgdev::row_ptr_of;
+using mrgdev::seg_store;
 
 struct FactArgs {
   Grid g;

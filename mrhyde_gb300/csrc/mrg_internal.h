@@ -108,6 +108,9 @@ struct mrg_problem {
   double* d_vcoord = nullptr;   // [nvert*dim] (general geometry) or null
   double* d_srcB = nullptr;     // per-axis source tables (factored path, sinprod source)
   double* d_qtab = nullptr;     // reference tables for the per-cell path: w, phi, dphi (+ geometric psi, dpsi)
+  double* d_khat = nullptr;     // stored-geometry path: [36][ncell] kappa-free symmetric cell stiffness
+  float* d_khat32 = nullptr;    // [36][ncell] FP32 copy (mixed-precision Jacobian)
+  double* d_bload = nullptr;    // [ndof] load vector b_i = sum over the node's cells of int f phi_i
   // host copies of small tables
   double Kp[8];                 // factored path: K(|dx|,|dy|,|dz|) of one cell, kappa = 1
   double cell_load;             // factored path: int_cell phi_l for one node (vol / 2^dim)
@@ -148,6 +151,10 @@ int mrg_q2tc_create(mrg_problem* p, const double* tab, const double s[3], Q2Tc**
 void mrg_q2tc_free(Q2Tc* T, cudaStream_t st);
 float* mrg_q2tc_w_image(Q2Tc* T);  // [tile][hi, lo][K chunk 28][cell 128][4] TF32 operand image
 int mrg_q2tc_launch(const mrg_problem* p, Q2Tc* T, float* J, bool ovw, int* err, cudaStream_t s);
+// Thermal Q1 hexahedra on general geometry from per-cell data stored at setup (mrg_stored.cu)
+bool mrg_stored_eligible(int dim, int order, int kind, int points_per_axis, bool affine);
+int mrg_stored_setup(mrg_problem* p, cudaStream_t s);
+int mrg_launch_stored(mrg_problem* p, const double* u, double* r, void* J, uint32_t flags, cudaStream_t s);
 // Face boundary terms (mrg_boundary.cu)
 void mrg_boundary_free(mrg_problem* p);
 bool mrg_boundary_active(const mrg_problem* p);

@@ -240,6 +240,9 @@ static void free_problem(mrg_problem* p) {
   cudaFreeAsync(p->d_vcoord, s);
   cudaFreeAsync(p->d_srcB, s);
   cudaFreeAsync(p->d_qtab, s);
+  cudaFreeAsync(p->d_khat, s);
+  cudaFreeAsync(p->d_khat32, s);
+  cudaFreeAsync(p->d_bload, s);
   cudaStreamSynchronize(s);
   delete p;
 }
@@ -316,6 +319,8 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
   else if (P->affine && m->dim == 3 && n1 == p + 1 && ph->source_kind == MRG_SRC_CONST &&
            (p == 2 || ph->kind == MRG_DIFFUSION_1PU2))
     P->path = MRG_PATH_TENSOR;
+  else if (mrg_stored_eligible(m->dim, p, ph->kind, n1, P->affine))
+    P->path = MRG_PATH_STORED;
   else
     P->path = MRG_PATH_CELL;
 
@@ -501,6 +506,7 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
   }
   int st = mrg_launch_kappa32(P, cs);
   if (st == MRG_OK && P->path == MRG_PATH_TENSOR) st = mrg_q2_setup(P);
+  if (st == MRG_OK && P->path == MRG_PATH_STORED) st = mrg_stored_setup(P, cs);
   if (st != MRG_OK) {
     free_problem(P);
     return st;
@@ -611,6 +617,9 @@ extern "C" int mrg_assemble(mrg_problem* p, const double* u, double* r, void* J,
     if (st != MRG_OK) return st;
   } else if (p->path == MRG_PATH_TENSOR && !(flags & MRG_ASM_FORCE_CELL)) {
     st = mrg_launch_q2(p, u, r, J, flags, s);
+    if (st != MRG_OK) return st;
+  } else if (p->path == MRG_PATH_STORED && !(flags & (MRG_ASM_FORCE_CELL | MRG_ASM_ATOMIC))) {
+    st = mrg_launch_stored(p, u, r, J, flags, s);
     if (st != MRG_OK) return st;
   } else {
     if (flags & MRG_ASM_OVERWRITE) {
