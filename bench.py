@@ -429,6 +429,7 @@ def targets_summary(out):
         t["general_noaffine"] = {"fp64_jacres_ms": r3(gen.get("fp64_jacres_ms")),
                                  "mixed_jacres_ms": r3(gen.get("mixed_jacres_ms")),
                                  "residual_ms": r3(gen.get("residual_ms")),
+                                 "ad_kernels_fp64_jacres_ms": r3(gen.get("ad_kernels_fp64_jacres_ms")),
                                  "hbm_frac_fp64": r3(gen.get("hbm_frac_fp64"))}
     c4 = out.get("c4") or {}
     if c4 and "error" not in c4:
@@ -535,13 +536,20 @@ def bench_general(args):
     from mrhyde_gb300.workloads import c2_general
 
     n = args.general_n
-    P = Problem(**c2_general(seed=2, n=n))
+    cfg = c2_general(seed=2, n=n)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    P = Problem(**cfg)  # creation computes and stores every cell's stiffness (the stored-geometry path)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
     info = P.info
     A = AssemblyManager(P)
     u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, info.n_dofs), device="cuda")
     r = P.new_vector()
     J64 = P.new_matrix_values(fp32=False)
     t64 = _ev_time(lambda: A.assembleJacRes(u, r, J64, overwrite=True), 3)
+    # the per-cell forward-AD kernels (geometry and AD tangents per cell, 8-colour scatter) on the same mesh
+    tad = _ev_time(lambda: A.assembleJacRes(u, r, J64, overwrite=True, force_cell=True), 2)
     del J64
     J32 = P.new_matrix_values(fp32=True)
     t32 = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True), 3)
@@ -555,6 +563,7 @@ def bench_general(args):
             "fp64_jacres_ms": t64, "fp64_cells_per_s": info.n_cells / (t64 * 1e-3),
             "mixed_jacres_ms": t32, "mixed_cells_per_s": info.n_cells / (t32 * 1e-3),
             "residual_ms": tres, "residual_cells_per_s": info.n_cells / (tres * 1e-3),
+            "ad_kernels_fp64_jacres_ms": tad, "setup_s": setup_s,
             "hbm_frac_fp64": algo / (t64 * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes": algo}
 
 
@@ -714,7 +723,8 @@ def run_profile(args, local_rank):
         torch.cuda.synchronize()
         print(json.dumps({"profile": "c4", "steps": args.steps, "ok": True}))
         return
-    if args.profile in ("cell64", "cell32"):  # the per-cell path on non-affine hexahedra (C2 coefficients)
+    if args.profile in ("cell64", "cell32", "cellad64"):  # non-affine hexahedra, C2 coefficients; cellad64
+        # forces the per-cell forward-AD kernels, the others take the default (stored-geometry) path
         from mrhyde_gb300.workloads import c2_general
 
         P = Problem(**c2_general(seed=2, n=args.general_n))
@@ -722,7 +732,8 @@ def run_profile(args, local_rank):
         u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, P.info.n_dofs), device="cuda")
         r, J = P.new_vector(), P.new_matrix_values(fp32=args.profile == "cell32")
         for _ in range(args.warmup + args.steps):
-            A.assembleJacRes(u, r, J, fp32_jacobian=args.profile == "cell32", overwrite=True)
+            A.assembleJacRes(u, r, J, fp32_jacobian=args.profile == "cell32", overwrite=True,
+                             force_cell=args.profile == "cellad64")
         torch.cuda.synchronize()
         print(json.dumps({"profile": args.profile, "n": args.general_n, "steps": args.steps, "ok": True}))
         return
@@ -781,7 +792,7 @@ def main():
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
     ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4",
-                             "cell64", "cell32"],
+                             "cell64", "cell32", "cellad64"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
