@@ -737,6 +737,19 @@ def run_profile(args, local_rank):
         torch.cuda.synchronize()
         print(json.dumps({"profile": args.profile, "n": args.general_n, "steps": args.steps, "ok": True}))
         return
+    if args.profile == "q2tcj":  # the Q2 FP32 Jacobian alone on the tensor cores (coefficients, contraction, rows)
+        from mrhyde_gb300.workloads import c3
+
+        cfg, u0 = c3(seed=3, n=args.c3_n)
+        P = Problem(**cfg)
+        A = AssemblyManager(P)
+        u = torch.tensor(u0, device="cuda")
+        J = P.new_matrix_values(fp32=True)
+        for _ in range(args.warmup + args.steps):
+            A.assembleJac(u, J, fp32_jacobian=True, overwrite=True, tensor_cores=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.profile, "n": args.c3_n, "steps": args.steps, "ok": True}))
+        return
     if args.profile in ("q2tc", "q2cc"):
         from mrhyde_gb300.workloads import c3
 
@@ -792,7 +805,7 @@ def main():
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
     ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4",
-                             "cell64", "cell32", "cellad64"],
+                             "cell64", "cell32", "cellad64", "q2tcj"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

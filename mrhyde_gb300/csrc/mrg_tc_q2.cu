@@ -52,7 +52,15 @@ constexpr int NCH = 256;          // columns per accumulator = MMA N
 constexpr int NNCH = NE / NCH;    // 3 accumulator slices per tile
 constexpr int KH = 112;           // H^T row length (K padded to a multiple of 8)
 constexpr int KW = 108;           // W row length in global memory
-constexpr int NBS = 5;            // H stages (K = 8 each)
+// H stages (K = 8 each) and epilogue staging buffers per epilogue warp
+#ifndef MRG_TC_NBS
+#define MRG_TC_NBS 6
+#endif
+#ifndef MRG_TC_EBUFS
+#define MRG_TC_EBUFS 1
+#endif
+constexpr int NBS = MRG_TC_NBS;
+constexpr int EBUFS = MRG_TC_EBUFS;
 constexpr int A_PLANE = TM * KH * 4;          // 57344 bytes per W plane (hi or lo)
 constexpr int B_PLANE = NCH * 8 * 4;          // 8192 bytes per H plane per stage
 constexpr int B_STAGE = 2 * B_PLANE;          // hi + lo
@@ -65,11 +73,16 @@ constexpr int H_STAGE_FLOATS = B_STAGE / 4;   // one (slice, K step) stage of H:
 constexpr int OFF_AH = 0;
 constexpr int OFF_AL = OFF_AH + A_PLANE;
 constexpr int OFF_B = OFF_AL + A_PLANE;                 // NBS stages of [hi | lo]
-constexpr int OFF_E = OFF_B + NBS * B_STAGE;            // 4 warps x 2 buffers (1024-byte aligned)
-constexpr int OFF_BAR = OFF_E + 4 * 2 * E_BUF;
-// barriers: a_full, a_empty, b_full[NBS], b_empty[NBS], t_full[2], t_empty[2], spare
-constexpr int BAR_A_FULL = 0, BAR_A_EMPTY = 1, BAR_B_FULL = 2, BAR_B_EMPTY = 2 + NBS, BAR_T_FULL = 2 + 2 * NBS,
-              BAR_T_EMPTY = 4 + 2 * NBS, BAR_SPARE = 6 + 2 * NBS, NBAR = 7 + 2 * NBS;
+constexpr int OFF_E = OFF_B + NBS * B_STAGE;            // 4 warps x EBUFS buffers (1024-byte aligned)
+constexpr int OFF_BAR = OFF_E + 4 * EBUFS * E_BUF;
+// barriers: a_full[K steps], a_empty[K steps] (one per 8-wide K chunk of the W tile, so the next tile's W
+// streams in while the last slice of the current tile still uses the later chunks), b_full[NBS],
+// b_empty[NBS], t_full[2], t_empty[2], spare
+constexpr int KS = KH / 8;
+constexpr int BAR_A_FULL = 0, BAR_A_EMPTY = KS, BAR_B_FULL = 2 * KS, BAR_B_EMPTY = 2 * KS + NBS,
+              BAR_T_FULL = 2 * KS + 2 * NBS, BAR_T_EMPTY = 2 * KS + 2 * NBS + 2, BAR_SPARE = 2 * KS + 2 * NBS + 4,
+              NBAR = 2 * KS + 2 * NBS + 5;
+constexpr int A_CHUNK = 2 * TM * 16;          // bytes of one K step (8 values) of one W plane
 constexpr int OFF_MISC = OFF_BAR + NBAR * 8;            // tmem address (4) + abort flag (4)
 constexpr int SMEM_USED = OFF_MISC + 16;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;            // slack for aligning the base to 1024 bytes
@@ -181,8 +194,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    mbar_init(bar(BAR_A_FULL), 1);
-    mbar_init(bar(BAR_A_EMPTY), 1);
+    for (int k = 0; k < KS; ++k) {
+      mbar_init(bar(BAR_A_FULL + k), 1);
+      mbar_init(bar(BAR_A_EMPTY + k), 1);
+    }
     for (int s = 0; s < NBS; ++s) {
       mbar_init(bar(BAR_B_FULL + s), 1);
       mbar_init(bar(BAR_B_EMPTY + s), 1);
@@ -205,7 +220,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const int kchunks = 2 * ksteps;  // 16-byte K chunks of W per tile
   const unsigned long long lim = wait_ns ? wait_ns : WAIT_NS;
 
   if (warp == 0) {
@@ -213,23 +227,27 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       bool ok = true;
       uint32_t bit = 0, ta = 0;
-      int a_armed = -1;
+      int a_armed[KS];
       int b_armed[NBS];
+      for (int k = 0; k < KS; ++k) a_armed[k] = -1;
       for (int s = 0; s < NBS; ++s) b_armed[s] = -1;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++ta) {
-        if (!mbar_wait(bar(BAR_A_EMPTY), (ta & 1u) ^ 1u, abort_flag, lim)) { ok = false; break; }
-        // withhold (testing): the W copy of tile 0 is never issued, so the MMA thread's wait for it runs
-        // out and the abort path is taken with no copy in flight on that barrier
-        if (!(withhold && tile == 0)) {
-          const uint32_t abytes = (uint32_t)(kchunks * TM * 16);
-          mbar_expect_tx(bar(BAR_A_FULL), 2u * abytes);
-          a_armed = (int)(ta & 1u);
-          const float* wt = wimg + (size_t)tile * W_TILE_FLOATS;
-          bulk_load(sAh, wt, abytes, bar(BAR_A_FULL));
-          bulk_load(sAl, wt + TM * KH, abytes, bar(BAR_A_FULL));
-        }
+        const float* wt = wimg + (size_t)tile * W_TILE_FLOATS;
         for (int n = 0; n < NNCH && ok; ++n)
           for (int ks = 0; ks < ksteps; ++ks, ++bit) {
+            if (n == 0) {
+              // K chunk ks of the tile's W (hi and lo planes), once its previous contents are consumed
+              if (!mbar_wait(bar(BAR_A_EMPTY + ks), (ta & 1u) ^ 1u, abort_flag, lim)) { ok = false; break; }
+              // withhold (testing): the W copies of tile 0 are never issued, so the MMA thread's wait for
+              // them runs out and the abort path is taken with no copy in flight on those barriers
+              if (!(withhold && tile == 0)) {
+                mbar_expect_tx(bar(BAR_A_FULL + ks), 2u * A_CHUNK);
+                a_armed[ks] = (int)(ta & 1u);
+                const size_t ko = (size_t)ks * (A_CHUNK / 4);
+                bulk_load(sAh + ks * A_CHUNK, wt + ko, A_CHUNK, bar(BAR_A_FULL + ks));
+                bulk_load(sAl + ks * A_CHUNK, wt + TM * KH + ko, A_CHUNK, bar(BAR_A_FULL + ks));
+              }
+            }
             const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
             if (!mbar_wait(bar(BAR_B_EMPTY + st), ph ^ 1u, abort_flag, lim)) { ok = false; break; }
             mbar_expect_tx(bar(BAR_B_FULL + st), (uint32_t)B_STAGE);
@@ -247,7 +265,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       if (!ok) {
         // copies in flight land on their full barriers: wait for the last phase armed on each
-        if (a_armed >= 0) mbar_wait_cleanup(bar(BAR_A_FULL), (uint32_t)a_armed);
+        for (int k = 0; k < KS; ++k)
+          if (a_armed[k] >= 0) mbar_wait_cleanup(bar(BAR_A_FULL + k), (uint32_t)a_armed[k]);
         for (int s = 0; s < NBS; ++s)
           if (b_armed[s] >= 0) mbar_wait_cleanup(bar(BAR_B_FULL + s), (uint32_t)b_armed[s]);
       }
@@ -259,14 +278,14 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true, issued = false;
       uint32_t bit = 0, acc = 0, ta = 0;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++ta) {
-        if (!mbar_wait(bar(BAR_A_FULL), ta & 1u, abort_flag, lim)) { ok = false; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const bool more = tile + (int)gridDim.x < ntiles;
         for (int n = 0; n < NNCH && ok; ++n, ++acc) {
           const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
           if (!mbar_wait(bar(BAR_T_EMPTY + buf), aph ^ 1u, abort_flag, lim)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
           const uint32_t d = tmem + buf * NCH;
           for (int ks = 0; ks < ksteps; ++ks, ++bit) {
+            if (n == 0 && !mbar_wait(bar(BAR_A_FULL + ks), ta & 1u, abort_flag, lim)) { ok = false; break; }
             const uint32_t st = bit % NBS, ph = (bit / NBS) & 1u;
             if (!mbar_wait(bar(BAR_B_FULL + st), ph, abort_flag, lim)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -279,10 +298,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             mma_tf32(d, dAl, dBh, 1u);
             issued = true;
             mma_commit(bar(BAR_B_EMPTY + st));
+            // after the last slice's use of W chunk ks, release it for the CTA's next tile
+            if (n == NNCH - 1 && more) mma_commit(bar(BAR_A_EMPTY + ks));
           }
           if (ok) mma_commit(bar(BAR_T_FULL + buf));
         }
-        if (ok && tile + (int)gridDim.x < ntiles) mma_commit(bar(BAR_A_EMPTY));
       }
       if (!ok && issued) {
         // let the MMAs already issued finish before TMEM is released
@@ -295,7 +315,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     // ------------------------------ epilogue (warps 2..5) ------------------------------
     const int q = warp & 3;           // TMEM lane quarter this warp may access
     const int ew = warp - 2;          // staging buffers of this warp
-    const uint32_t stg0 = sE + (uint32_t)ew * 2u * E_BUF;
+    const uint32_t stg0 = sE + (uint32_t)ew * (uint32_t)EBUFS * E_BUF;
     bool ok = true;
     uint32_t acc = 0, piece = 0;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
@@ -321,9 +341,12 @@ __global__ void __launch_bounds__(THREADS, 1)
               : "r"(taddr)
               : "memory");
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-          const uint32_t stg = stg0 + (piece & 1u) * E_BUF;
-          // the store issued from this buffer two pieces ago must have finished reading it
-          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
+          const uint32_t stg = stg0 + (piece % (uint32_t)EBUFS) * E_BUF;
+          // the store issued from this buffer EBUFS pieces ago must have finished reading it
+          if (lane == 0) {
+            if constexpr (EBUFS == 2) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
+            else asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+          }
           __syncwarp();
           // row = lane (128 bytes); 16-byte chunk c goes to chunk position c ^ (row & 7) (128B swizzle)
 #pragma unroll
