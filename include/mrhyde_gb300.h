@@ -236,7 +236,10 @@ typedef struct mrg_newton_opts {
   int32_t lin_maxiter;
   int32_t reuse_jacobian; /* 1: assemble J once (linear problems)                              */
   int32_t krylov;       /* MRG_KRYLOV_*: AUTO = PCG for the symmetric thermal form, BiCGStab for 1+u^2 */
-  int32_t reserved;
+  int32_t gmg_full_setup; /* multigrid preconditioner and a re-assembled Jacobian: 1 rebuilds every level at
+                             every Newton step; 0 (default) rebuilds the coarse Galerkin operators only at the
+                             first step and when the previous Krylov solve needed more iterations than the one
+                             right after the last full setup, level 0 always follows the new Jacobian */
 } mrg_newton_opts;
 
 /* Newton on F(u) = 0 with u on device (holding the initial guess; Dirichlet values are set first).

@@ -70,7 +70,7 @@ MRG_PREC_JACOBI, MRG_PREC_GMG, MRG_PREC_GMG_SPLIT = 0, 1, 2
 class NewtonOpts(C.Structure):
     _fields_ = [("nl_tol", C.c_double), ("max_iters", C.c_int32), ("mixed", C.c_int32),
                 ("lin_tol", C.c_double), ("lin_maxiter", C.c_int32), ("reuse_jacobian", C.c_int32),
-                ("krylov", C.c_int32), ("reserved", C.c_int32)]
+                ("krylov", C.c_int32), ("gmg_full_setup", C.c_int32)]
 
 
 class BatchDesc(C.Structure):

@@ -1249,6 +1249,19 @@ template <typename T>
 constexpr int staged_smem() { return (NT / 32) * 2 * wbuf_elems<T>() * (int)sizeof(T); }
 
 // Level operators, diagonals, Gershgorin bounds and the coarsest inverse for the Jacobian J.
+// Level 0 only: the new J, its Jacobi inverse and Chebyshev bound; the coarse levels stay as they are.
+template <typename T>
+int setup_level0(Hier<T>* H, const T* J, cudaStream_t s) {
+  HLevel& L = H->L[0];
+  L.A = const_cast<T*>(J);
+  MRG_CUDA(cudaMemsetAsync(H->lmax, 0, sizeof(unsigned int), s));
+  if (L.pp.p[0] == 2) k_diag<2, T><<<nblk(L.n, NT), NT, 0, s>>>(L.g, (const T*)L.A, (T*)L.minv, H->lmax);
+  else k_diag<1, T><<<nblk(L.n, NT), NT, 0, s>>>(L.g, (const T*)L.A, (T*)L.minv, H->lmax);
+  k_cheb_coef<<<1, 32, 0, s>>>(H->lmax, (int)H->L.size(), H->coef);
+  MRG_CUDA(cudaGetLastError());
+  return MRG_OK;
+}
+
 template <typename T>
 int setup_values(Hier<T>* H, const T* J, cudaStream_t s) {
   H->L[0].A = const_cast<T*>(J);
@@ -1396,17 +1409,27 @@ int finish_solve(mrg_problem* p, Hier<T>* H, cudaGraphExec_t graph, double* x, d
   return MRG_OK;
 }
 
+// Brings the hierarchy up to date with J as the caller asks (MRG_GMG_SETUP_*); a J other than the one of
+// the last setup always gets a full setup.
 template <typename T>
-int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
-           mrg_solve_stats* st, bool reuse, cudaStream_t s) {
-  int rc = set_staged_attr<T>();
-  if (rc) return rc;
-  // the level operators are rebuilt unless the caller guarantees J is unchanged since the last setup
-  if (!reuse || H->setup_J != (const void*)J) {
-    rc = setup_values(H, J, s);
+int follow_j(Hier<T>* H, const T* J, int setup, cudaStream_t s) {
+  if (setup == MRG_GMG_SETUP_FULL || H->setup_J != (const void*)J) {
+    const int rc = setup_values(H, J, s);
     if (rc) return rc;
     H->setup_J = J;
+  } else if (setup == MRG_GMG_SETUP_LEVEL0) {
+    return setup_level0(H, J, s);
   }
+  return MRG_OK;
+}
+
+template <typename T>
+int gmg_cg(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
+           mrg_solve_stats* st, int setup, cudaStream_t s) {
+  int rc = set_staged_attr<T>();
+  if (rc) return rc;
+  rc = follow_j(H, J, setup, s);
+  if (rc) return rc;
   set_tail(H, gdata(p)->split);
   GScal init{};
   init.tol = rtol;
@@ -1469,19 +1492,15 @@ void enqueue_bg_iters(Hier<T>* H, int count, cudaStream_t s) {
 
 template <typename T>
 int gmg_bicgstab(mrg_problem* p, Hier<T>* H, const T* J, const double* b, double* x, double rtol, int maxiter,
-                 mrg_solve_stats* st, bool reuse, cudaStream_t s) {
+                 mrg_solve_stats* st, int setup, cudaStream_t s) {
   int rc = set_staged_attr<T>();
   if (rc) return rc;
   const int64_t n = p->ndof;
   if (!H->rh)
     for (T** ptr : {&H->rh, &H->v, &H->sv, &H->t, &H->ph, &H->sh})
       if (cudaMallocAsync(ptr, n * sizeof(T), s) != cudaSuccess) return mrg_fail(MRG_ENOMEM, "multigrid BiCGStab vectors");
-  // the level operators are rebuilt unless the caller guarantees J is unchanged since the last setup
-  if (!reuse || H->setup_J != (const void*)J) {
-    rc = setup_values(H, J, s);
-    if (rc) return rc;
-    H->setup_J = J;
-  }
+  rc = follow_j(H, J, setup, s);
+  if (rc) return rc;
   set_tail(H, gdata(p)->split);
   GScal init{};
   init.tol = rtol;
@@ -1540,30 +1559,30 @@ void mrg_gmg_free(mrg_problem* p) {
 // Solves J x = b (x0 = 0) with multigrid-preconditioned CG in the precision of J; x receives the FP64
 // solution.
 int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                  mrg_solve_stats* st, bool reuse_setup, cudaStream_t s) {
+                  mrg_solve_stats* st, int setup, cudaStream_t s) {
   if (p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 and Q2 problems only");
   GmgData* G = gdata(p);
   int rc;
   if (fp32) {
     if (!G->h32 && (rc = build_hier<float>(p, G->h32, s))) return rc;
-    return gmg_cg<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, reuse_setup, s);
+    return gmg_cg<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, setup, s);
   }
   if (!G->h64 && (rc = build_hier<double>(p, G->h64, s))) return rc;
-  return gmg_cg<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, reuse_setup, s);
+  return gmg_cg<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, setup, s);
 }
 
 // Same for a nonsymmetric J: right-preconditioned BiCGStab with the multigrid V-cycle.
 int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                     mrg_solve_stats* st, bool reuse_setup, cudaStream_t s) {
+                     mrg_solve_stats* st, int setup, cudaStream_t s) {
   if (p->g.p > 2) return mrg_fail(MRG_ENOTSUP, "multigrid: Q1 and Q2 problems only");
   GmgData* G = gdata(p);
   int rc;
   if (fp32) {
     if (!G->h32 && (rc = build_hier<float>(p, G->h32, s))) return rc;
-    return gmg_bicgstab<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, reuse_setup, s);
+    return gmg_bicgstab<float>(p, G->h32, (const float*)J, b, x, rtol, maxiter, st, setup, s);
   }
   if (!G->h64 && (rc = build_hier<double>(p, G->h64, s))) return rc;
-  return gmg_bicgstab<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, reuse_setup, s);
+  return gmg_bicgstab<double>(p, G->h64, (const double*)J, b, x, rtol, maxiter, st, setup, s);
 }
 
 extern "C" int mrg_set_preconditioner(mrg_problem* p, int32_t kind) {

@@ -164,11 +164,15 @@ void mrg_lagrange_1d(int p, double xi, double* l, double* dl);
 // Multigrid preconditioned CG (mrg_gmg.cu)
 int mrg_gmg_kind(const mrg_problem* p);
 void mrg_gmg_free(mrg_problem* p);
-// reuse_setup: J is unchanged since the last solve with the same pointer (skip the hierarchy setup)
+// setup: how the hierarchy follows J.  FULL rebuilds every level; REUSE keeps everything (J unchanged
+// since the last setup); LEVEL0 refreshes level 0 (J itself, its diagonal and Chebyshev bound) and keeps
+// the coarse Galerkin operators of the last full setup (a lagged preconditioner; the Krylov operator is
+// always the current J).
+enum { MRG_GMG_SETUP_FULL = 0, MRG_GMG_SETUP_REUSE = 1, MRG_GMG_SETUP_LEVEL0 = 2 };
 int mrg_gmg_solve(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                  mrg_solve_stats* st, bool reuse_setup, cudaStream_t s);
+                  mrg_solve_stats* st, int setup, cudaStream_t s);
 int mrg_gmg_bicgstab(mrg_problem* p, const void* J, bool fp32, const double* b, double* x, double rtol, int maxiter,
-                     mrg_solve_stats* st, bool reuse_setup, cudaStream_t s);
+                     mrg_solve_stats* st, int setup, cudaStream_t s);
 // Solver (mrg_solver.cu)
 void mrg_solver_free(mrg_problem* p);
 void mrg_solver_drop_graphs(mrg_problem* p);  // captured PCG chunks (recaptured on next use)

@@ -761,6 +761,7 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
   if (rc) return rc;
   double first = 0.0, scaled = 1.0, nrm = 0.0, alpha = 1.0;
   int it = 0, cgtot = 0;
+  int full_iters = -1, last_iters = 0;  // Krylov iterations after the last full multigrid setup / last solve
   bool proceed = true, have_J = false, have_du = false;
   int status = MRG_OK;
   while (proceed) {
@@ -796,9 +797,19 @@ extern "C" int mrg_newton(mrg_problem* p, double* u, const mrg_newton_opts* o, m
       // the 1+u^2 Jacobian is nonsymmetric (2 u phi_j grad u . grad phi_i): BiCGStab; CG otherwise
       const bool bicg = (o->krylov == MRG_KRYLOV_BICGSTAB) || (o->krylov == MRG_KRYLOV_AUTO && p->kind != MRG_THERMAL);
       if (mrg_gmg_kind(p) == MRG_PREC_GMG) {
-        rc = bicg ? mrg_gmg_bicgstab(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, !fresh, s)
-                  : mrg_gmg_solve(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, !fresh, s);
+        // A re-assembled J gets a full multigrid setup at the first solve and whenever the previous solve
+        // needed more Krylov iterations than the one right after the last full setup; otherwise only level 0
+        // follows J and the coarse Galerkin operators are kept (their setup costs more than a Krylov
+        // iteration; late Newton steps change J little).  opts.gmg_full_setup forces a full setup.
+        int setup = MRG_GMG_SETUP_REUSE;
+        if (fresh)
+          setup = (o->gmg_full_setup || full_iters < 0 || last_iters > full_iters) ? MRG_GMG_SETUP_FULL
+                                                                                     : MRG_GMG_SETUP_LEVEL0;
+        rc = bicg ? mrg_gmg_bicgstab(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, setup, s)
+                  : mrg_gmg_solve(p, J, mixed, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, setup, s);
         if (rc && rc != MRG_ENOCONV && !(bicg && rc == MRG_ENUMERIC)) return rc;
+        if (setup == MRG_GMG_SETUP_FULL) full_iters = ls.iterations;
+        last_iters = ls.iterations;
       } else if (!mixed) {
         MRG_CUDA(cudaMemsetAsync(w->du, 0, p->ndof * sizeof(double), s));
         rc = bicg ? mrg_bicg_solve64(p, w->J64, w->F, w->du, o->lin_tol, o->lin_maxiter, &ls, s)

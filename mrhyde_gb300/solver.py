@@ -33,7 +33,7 @@ def _result(st: L.SolveStats) -> SolveResult:
 class SolverManager:
     def __init__(self, problem: Problem, nonlinear_tol=1.0e-6, max_nonlinear_iters=10, linear_tol=1.0e-7,
                  linear_maxiter=100000, mixed_precision=False, reuse_jacobian=False, krylov="auto",
-                 preconditioner="jacobi"):
+                 preconditioner="jacobi", gmg_full_setup=False):
         self.problem = problem
         self.NLtol = nonlinear_tol
         self.maxNLiter = max_nonlinear_iters
@@ -41,6 +41,9 @@ class SolverManager:
         self.linear_maxiter = linear_maxiter
         self.mixed = mixed_precision
         self.reuse_jacobian = reuse_jacobian
+        # multigrid with a re-assembled Jacobian: True rebuilds every level at every Newton step; False keeps
+        # the coarse Galerkin operators while the Krylov iteration count does not grow (mrg_newton_opts)
+        self.gmg_full_setup = gmg_full_setup
         self.krylov = {"auto": L.MRG_KRYLOV_AUTO, "pcg": L.MRG_KRYLOV_PCG, "bicgstab": L.MRG_KRYLOV_BICGSTAB}[krylov]
         # "jacobi": the reference's SolverManager::PCG; "gmg": geometric multigrid V-cycle (Q1 and Q2),
         # the structured-grid counterpart of the reference's Belos + MueLu option; "gmg_split": the same
@@ -106,6 +109,7 @@ class SolverManager:
         o.lin_maxiter = self.linear_maxiter
         o.reuse_jacobian = int(self.reuse_jacobian)
         o.krylov = self.krylov
+        o.gmg_full_setup = int(self.gmg_full_setup)
         st = L.SolveStats()
         rc = L.lib().mrg_newton(self.problem.handle, _ptr(u), C.byref(o), C.byref(st), _stream(stream))
         if rc != L.MRG_OK and (raise_on_noconv or rc != L.MRG_ENOCONV):
