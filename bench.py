@@ -39,9 +39,9 @@ WORKLOAD = ("C2: steady thermal, unit cube, 128^3 Q1 hex (2,097,152 cells, 8 nod
             "kappa=exp(0.5 g) per cell, f=1, u=0 on x=0 and x=1, one Jacobian+residual assembly per step")
 
 
-def algorithmic_bytes(ncell, nnode, nnz, s_j, npe=8):
+def algorithmic_bytes(ncell, nnode, nnz, s_j, npe=8, dim=3):
     """Bytes one Q1 Jac+res assembly must move: J values, u and r, kappa and connectivity, coordinates."""
-    return nnz * s_j + nnode * (8 + 8) + ncell * (8 + 4 * npe) + nnode * 24
+    return nnz * s_j + nnode * (8 + 8) + ncell * (8 + 4 * npe) + nnode * 8 * dim
 
 
 def read_peaks():
@@ -374,7 +374,8 @@ def run_ours(args, rank, world, local_rank):
         out["solve"] = sol
 
     if not args.no_extras:
-        for name, fn in (("general", bench_general), ("c3", bench_c3), ("c4", bench_c4),
+        for name, fn in (("general", bench_general), ("general_quad", bench_general_quad), ("c3", bench_c3),
+                         ("c4", bench_c4),
                          ("c5", lambda a: bench_c5(a, rank, world, dist))):
             try:
                 out[name] = fn(args)
@@ -431,6 +432,10 @@ def targets_summary(out):
                                  "residual_ms": r3(gen.get("residual_ms")),
                                  "ad_kernels_fp64_jacres_ms": r3(gen.get("ad_kernels_fp64_jacres_ms")),
                                  "hbm_frac_fp64": r3(gen.get("hbm_frac_fp64"))}
+    gq = out.get("general_quad") or {}
+    if gq and "error" not in gq:
+        t["general_noaffine_quad"] = {k: r3(gq.get(k)) for k in ("fp64_jacres_ms", "mixed_jacres_ms", "residual_ms",
+                                                                 "ad_kernels_fp64_jacres_ms", "hbm_frac_fp64")}
     c4 = out.get("c4") or {}
     if c4 and "error" not in c4:
         t["c4"] = {"ms_per_batch": r3(c4.get("ms_per_batch")), "all_converged": c4.get("all_converged")}
@@ -564,6 +569,42 @@ def bench_general(args):
             "mixed_jacres_ms": t32, "mixed_cells_per_s": info.n_cells / (t32 * 1e-3),
             "residual_ms": tres, "residual_cells_per_s": info.n_cells / (tres * 1e-3),
             "ad_kernels_fp64_jacres_ms": tad, "setup_s": setup_s,
+            "hbm_frac_fp64": algo / (t64 * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes": algo}
+
+
+def bench_general_quad(args):
+    """C1's coefficients, source and boundary data on n^2 non-affine quadrilaterals (interior vertices moved
+    by up to 0.2 h): the stored-geometry path in 2-D, beside the per-cell forward-AD kernels."""
+    import torch
+
+    from mrhyde_gb300 import AssemblyManager, Problem
+    from mrhyde_gb300.workloads import c1_general
+
+    n = args.general_quad_n
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    P = Problem(**c1_general(seed=1, n=n))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    info = P.info
+    A = AssemblyManager(P)
+    u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, info.n_dofs), device="cuda")
+    r = P.new_vector()
+    J64 = P.new_matrix_values(fp32=False)
+    t64 = _ev_time(lambda: A.assembleJacRes(u, r, J64, overwrite=True), 3)
+    tad = _ev_time(lambda: A.assembleJacRes(u, r, J64, overwrite=True, force_cell=True), 2)
+    del J64
+    J32 = P.new_matrix_values(fp32=True)
+    t32 = _ev_time(lambda: A.assembleJacRes(u, r, J32, fp32_jacobian=True, overwrite=True), 3)
+    del J32
+    tres = _ev_time(lambda: A.assembleRes(u, r, overwrite=True), 3)
+    torch.cuda.empty_cache()
+    peaks, _ = read_peaks()
+    algo = algorithmic_bytes(info.n_cells, info.n_dofs, info.nnz, 8, npe=4, dim=2)
+    return {"workload": f"{n}^2 Q1 quadrilaterals, interior vertices perturbed by up to 0.2 h (non-affine), "
+                        "C1 coefficients", "path": info.path, "cells": info.n_cells, "dofs": info.n_dofs,
+            "nnz": info.nnz, "fp64_jacres_ms": t64, "fp64_cells_per_s": info.n_cells / (t64 * 1e-3),
+            "mixed_jacres_ms": t32, "residual_ms": tres, "ad_kernels_fp64_jacres_ms": tad, "setup_s": setup_s,
             "hbm_frac_fp64": algo / (t64 * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes": algo}
 
 
@@ -802,6 +843,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the C3/C4/C5 measurements")
     ap.add_argument("--c3-n", type=int, default=64)
     ap.add_argument("--general-n", type=int, default=128, help="cells per axis of the non-affine mesh leg")
+    ap.add_argument("--general-quad-n", type=int, default=2048,
+                    help="cells per axis of the non-affine quadrilateral leg")
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
     ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4",

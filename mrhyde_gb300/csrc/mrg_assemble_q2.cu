@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <vector>
 
+#include "mrg_fixmul.cuh"
 #include "mrg_internal.h"
 
 namespace {
@@ -79,6 +80,11 @@ __device__ __forceinline__ float tf32_rn(float x) {
   asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
 }
+
+// FP32 value of an interpolated quantity: FP32 stages pass it through, FP64 stages round it to nearest
+// on the integer pipes (the conversion instruction issues at the FP64 rate)
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(double v) { return mrgfix::f64_to_f32_rn(v); }
 
 // mode bits: 1 = scatter residual, 2 = store qp coefficients (QT precision).  CT = arithmetic type of
 // the interpolation stages: double for every pass that scatters the residual; float for the pass that
@@ -185,8 +191,8 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
         if constexpr (sizeof(QT) == 4) {
           if (tc_image) {
             // split of the FP32 value (the remainder is exact in FP32; 3xTF32 keeps ~22 bits anyway):
-            // one FP64 -> FP32 conversion per value, the rest on the FP32 pipe
-            const float f = (float)v;
+            // one FP64 -> FP32 rounding per value, on the integer pipes, the rest on the FP32 pipe
+            const float f = to_f32(v);
             const float hi = tf32_rn(f);
             float* t = qbuf + (cid >> 7) * (2 * 128 * 112) + (k >> 2) * 512 + (cid & 127) * 4 + (k & 3);
             t[0] = hi;
@@ -194,7 +200,8 @@ __global__ void __launch_bounds__(RW * 32) k_tp_res(const TPTabs T, Grid g, int 
             return;
           }
         }
-        qb[k] = (QT)v;
+        if constexpr (sizeof(QT) == 4) qb[k] = to_f32(v);
+        else qb[k] = (QT)v;
       };
       put(l, cw);
       if (kind != MRG_THERMAL) {

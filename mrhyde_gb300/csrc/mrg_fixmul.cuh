@@ -58,4 +58,30 @@ __host__ __device__ __forceinline__ uint64_t mul_bits(uint64_t mk, uint64_t ms, 
   return ((E - 1) << 52) + m;
 }
 
+// RN(x) as an FP32 bit pattern (nearest, ties to even) for an FP64 bit pattern b whose biased exponent
+// lies in [897, 1150], i.e. whose magnitude is in [2^-126, 2^128): the 8-bit exponent is the FP64 one
+// rebiased (1023 -> 127), the 23-bit significand its top 23 bits, and the 29 bits dropped round it, a
+// carry into the exponent included (the largest values round to infinity as IEEE 754 prescribes).  About
+// ten integer operations, where the FP64 -> FP32 conversion instruction issues at the FP64 rate.  Returns
+// false for every other exponent (zero, subnormal, underflowing, overflowing, infinite or NaN input),
+// which the caller converts with the conversion instruction.
+__host__ __device__ __forceinline__ bool f64_to_f32_bits(uint64_t b, uint32_t& out) {
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  if (e - 897u > 253u) return false;
+  uint32_t f = (hi & 0x80000000u) | (((hi & 0x7fffffffu) - (896u << 20)) << 3) | (lo >> 29);
+  // dropped bits rem < 2^29: round up iff rem > 2^28, or rem == 2^28 and f is odd
+  f += ((lo & 0x1fffffffu) + (f & 1u) + 0x0fffffffu) >> 29;
+  out = f;
+  return true;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  uint32_t f;
+  if (f64_to_f32_bits((uint64_t)__double_as_longlong(x), f)) return __uint_as_float(f);
+  return __double2float_rn(x);
+}
+#endif
+
 }  // namespace mrgfix

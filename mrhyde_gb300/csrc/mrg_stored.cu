@@ -1,4 +1,5 @@
-// Thermal assembly on general (non-affine) Q1 hexahedra from per-cell geometry stored at setup.
+// Thermal assembly on general (non-affine) Q1 hexahedra and quadrilaterals from per-cell geometry stored
+// at setup.
 //
 // The reference keeps, for every cell, its physical basis values, gradients and quadrature weights
 // computed once at setup: AssemblyManager::allocateGroupStorage -> Group::computeBasis for every group
@@ -20,6 +21,10 @@
 // residual-only pass, which the mixed pass also runs for its residual) the per-cell form above (72
 // FMAs).  The two agree to rounding; each pass is deterministic.
 //
+// Quadrilaterals store 10 values a cell, FP64 only (80 bytes a cell; k_geo_quad, k_node_load_quad), and
+// take one thread per 9-entry row (k_stored_quad), whose Jacobian passes, the mixed one included, form
+// the row in FP64 and take the residual from it.
+//
 // Geometry in k_geo_hex: with C the cofactor matrix of the geometric Jacobian J_q (J[k][m] = dx_k/dxi_m),
 // J^{-T} = C / det, so grad phi_i . grad phi_j w |det| = ghat_i^T (C^T C) ghat_j * w / |det| for the
 // reference gradients ghat: one symmetric 3 x 3 metric per quadrature point instead of eight physical
@@ -27,6 +32,7 @@
 #include <type_traits>
 
 #include "mrg_device.cuh"
+#include "mrg_fixmul.cuh"
 #include "mrg_internal.h"
 
 namespace {
@@ -58,13 +64,13 @@ static_assert(sym8(7, 7) == 35 && sym8(0, 7) == 7 && sym8(1, 1) == 8, "triangle 
 struct GeoArgs {
   Grid g;
   QTab tab;
-  const double* vcoord;  // [nvert][3], x fastest
+  const double* vcoord;  // [nvert][dim], x fastest
   int src_sin;
   double amp, freq;
   int64_t ncell;
-  double* khat;          // [36][ncell]
-  float* khat32;         // [36][ncell]
-  double* bload;         // [8][ncell] cell loads (summed per node by k_node_load)
+  double* khat;          // [36][ncell] (hexahedra) or [10][ncell] (quadrilaterals)
+  float* khat32;         // [36][ncell], hexahedra only
+  double* bload;         // [8 or 4][ncell] cell loads (summed per node by k_node_load / k_node_load_quad)
 };
 
 // 8 threads per cell: thread t first evaluates the geometry at quadrature point t, then row t of Khat.
@@ -363,7 +369,175 @@ __global__ void __launch_bounds__(ST_T, stored_minb<JT, DOJ, DOR>())
   }
 }
 
+// ---- quadrilaterals (2-D): 4 nodes and 4 Gauss points a cell, 10 symmetric stiffness values, 9-entry rows
+
+// index of (i, j), i <= j, in the row-major upper triangle of a 4 x 4 symmetric matrix
+__host__ __device__ constexpr int sym4(int i, int j) {
+  return i <= j ? i * 4 - (i * (i - 1)) / 2 + (j - i) : j * 4 - (j * (j - 1)) / 2 + (i - j);
+}
+static_assert(sym4(3, 3) == 9 && sym4(0, 3) == 3 && sym4(1, 1) == 4, "triangle layout");
+
+constexpr int GEO2_CPB = 32;  // cells per CTA of the 2-D setup kernel (4 threads each)
+
+// 4 threads per cell: thread t evaluates the geometry at Gauss point t, then row t of Khat.  With C the
+// cofactor matrix of the 2 x 2 geometric Jacobian, grad phi_i . grad phi_j w |det| = ghat_i^T C^T C ghat_j
+// w / |det|.
+__global__ void __launch_bounds__(GEO2_CPB * 4) k_geo_quad(const GeoArgs A) {
+  __shared__ double s_x[GEO2_CPB][4][2];
+  __shared__ double s_m[GEO2_CPB][4][3];  // w / |det| * C^T C: xx, yy, xy
+  __shared__ double s_fw[GEO2_CPB][4];
+  const int slot = threadIdx.x >> 2, t = threadIdx.x & 3;
+  const int64_t c = (int64_t)blockIdx.x * GEO2_CPB + slot;
+  const bool active = c < A.ncell;
+  const Grid& g = A.g;
+  if (active) {
+    const int cx = (int)(c % g.nc[0]), cy = (int)(c / g.nc[0]);
+    const int64_t vid = (cx + (t & 1)) + (int64_t)(g.nc[0] + 1) * (cy + (t >> 1));
+    s_x[slot][t][0] = __ldg(A.vcoord + vid * 2);
+    s_x[slot][t][1] = __ldg(A.vcoord + vid * 2 + 1);
+  }
+  __syncthreads();
+  if (active) {
+    const int q = t;
+    double Jm[2][2] = {{0, 0}, {0, 0}}, xq[2] = {0, 0};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double ps = A.tab.psi[v * 4 + q];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const double xv = s_x[slot][v][k];
+        xq[k] = fma(xv, ps, xq[k]);
+#pragma unroll
+        for (int m = 0; m < 2; ++m) Jm[k][m] = fma(xv, A.tab.dpsi[(v * 4 + q) * 2 + m], Jm[k][m]);
+      }
+    }
+    // cofactors C[k][m] = (-1)^(k+m) minor(k, m)
+    const double C00 = Jm[1][1], C01 = -Jm[1][0], C10 = -Jm[0][1], C11 = Jm[0][0];
+    const double det = Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0];
+    const double ad = fabs(det), w = A.tab.w[q];
+    const double sc = w / ad;
+    s_m[slot][q][0] = (C00 * C00 + C10 * C10) * sc;
+    s_m[slot][q][1] = (C01 * C01 + C11 * C11) * sc;
+    s_m[slot][q][2] = (C00 * C01 + C10 * C11) * sc;
+    double f = A.amp;
+    if (A.src_sin) f *= sin(A.freq * xq[0]) * sin(A.freq * xq[1]);
+    s_fw[slot][q] = f * w * ad;
+  }
+  __syncthreads();
+  if (!active) return;
+  const int i = t;
+  double kr[4] = {0, 0, 0, 0}, bl = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const double* M = s_m[slot][q];
+    const double g0 = A.tab.dphi[(i * 4 + q) * 2], g1 = A.tab.dphi[(i * 4 + q) * 2 + 1];
+    const double v0 = M[0] * g0 + M[2] * g1, v1 = M[2] * g0 + M[1] * g1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double* gj = A.tab.dphi + (j * 4 + q) * 2;
+      kr[j] = fma(v0, gj[0], fma(v1, gj[1], kr[j]));
+    }
+    bl = fma(A.tab.phi[i * 4 + q], s_fw[slot][q], bl);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (j >= i) A.khat[(int64_t)sym4(i, j) * A.ncell + c] = kr[j];
+  A.bload[(int64_t)i * A.ncell + c] = bl;
+}
+
+__global__ void k_node_load_quad(Grid g, int64_t nrows, int64_t ncell, const double* __restrict__ bload,
+                                 double* __restrict__ b) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nrows) return;
+  const int ix = (int)(n % g.nn[0]), iy = (int)(n / g.nn[0]);
+  double s = 0.0;
+  for (int by = 0; by < 2; ++by)
+    for (int bx = 0; bx < 2; ++bx) {
+      const int cx = ix - 1 + bx, cy = iy - 1 + by;
+      if (cx < 0 || cy < 0 || cx >= g.nc[0] || cy >= g.nc[1]) continue;
+      s += bload[((1 - bx) | ((1 - by) << 1)) * ncell + cx + (int64_t)g.nc[0] * cy];
+    }
+  b[n] = s;
+}
+
+// One CSR row (at most 9 entries) per thread.  The row is formed in FP64 for both Jacobian types and
+// rounded once when stored (an FP32 row would carry its rounding relative to the row's terms, which cancel
+// across the two cells sharing an edge of a distorted mesh), so every Jacobian pass, the mixed one
+// included, takes its residual from the FP64 row, r = b - J u (16 + 9 FMAs a row), and the residual-only
+// pass the per-cell form (20 FMAs).  Both are bound by FP64 issue.
+template <typename JT, bool DOJ, bool DOR, bool OVW>
+__global__ void __launch_bounds__(ST_T) k_stored_quad(const StoredArgs A, const double* __restrict__ u,
+                                                      double* __restrict__ r, JT* __restrict__ J) {
+  constexpr bool ROW64 = DOJ, CELLRES = DOR && !DOJ;
+  const int64_t n = (int64_t)blockIdx.x * ST_T + threadIdx.x;
+  if (n >= A.nrows) return;
+  const Grid& g = A.g;
+  const int NX = g.nn[0];
+  const int ix = (int)(n % NX), iy = (int)(n / NX);
+  const RowInfo R = row_info<1>(g, ix, iy, 0);
+  if (node_fixed(g, ix, iy, 0)) {
+    if (DOJ) {
+      const int len = R.cx * R.cy;
+      const int dp = (iy - R.ly) * R.cx + (ix - R.lx);
+      if (OVW) for (int k = 0; k < len; ++k) J[R.rp + k] = (k == dp) ? JT(1) : JT(0);
+      else J[R.rp + dp] = JT(1);
+    }
+    if (DOR && OVW) r[n] = 0.0;
+    return;
+  }
+  const int64_t nc = A.ncell;
+  const int xlo = R.lx - ix, ylo = R.ly - iy;
+  double a64[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) a64[k] = 0.0;
+  double res = CELLRES ? __ldg(A.bnode + n) : 0.0;
+#pragma unroll
+  for (int co = 0; co < 4; ++co) {
+    const int bx = co & 1, by = co >> 1;
+    const int cx = ix - 1 + bx, cy = iy - 1 + by;
+    const bool valid = cx >= 0 && cy >= 0 && cx < g.nc[0] && cy < g.nc[1];
+    const int64_t c = (valid ? cx : 0) + (int64_t)g.nc[0] * (valid ? cy : 0);
+    const int l = (1 - bx) | ((1 - by) << 1);
+    const double k64 = valid ? __ldg(A.kap + c) : 0.0;
+    double dot = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int jx = j & 1, jy = j >> 1;
+      const int s = (by + jy) * 3 + (bx + jx);  // (dy + 1) * 3 + (dx + 1)
+      const double kh = __ldg(A.khat + sym4(l, j) * nc + c);
+      if (ROW64) a64[s] = fma(k64, kh, a64[s]);
+      if (CELLRES && valid) dot = fma(kh, __ldg(u + (cx + jx) + (int64_t)NX * (cy + jy)), dot);
+    }
+    if (CELLRES) res = fma(-k64, dot, res);
+  }
+  double ju = 0.0;
+#pragma unroll
+  for (int s = 0; s < 9; ++s) {
+    const int dx = s % 3 - 1, dy = s / 3 - 1;
+    if (dx >= xlo && dx < xlo + R.cx && dy >= ylo && dy < ylo + R.cy) {
+      if (ROW64 && DOR) ju = fma(a64[s], __ldg(u + n + dx + (int64_t)NX * dy), ju);
+      if (DOJ) {
+        const int64_t pos = R.rp + (dy - ylo) * R.cx + (dx - xlo);
+        // FP32: rounded on the integer pipes (the conversion instruction issues at the FP64 rate)
+        const JT v = sizeof(JT) == 4 ? (JT)mrgfix::f64_to_f32_rn(a64[s]) : (JT)a64[s];
+        if (OVW) J[pos] = v; else J[pos] += v;
+      }
+    }
+  }
+  if (DOR) {
+    const double rv = CELLRES ? res : __ldg(A.bnode + n) - ju;
+    if (OVW) r[n] = rv; else r[n] += rv;
+  }
+}
+
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <typename JT, bool DOJ, bool DOR, bool OVW>
+cudaError_t launch_stored_quad(const mrg_problem* p, const StoredArgs& A, const double* u, double* r, JT* J,
+                               cudaStream_t s) {
+  k_stored_quad<JT, DOJ, DOR, OVW><<<nblk(p->ndof, ST_T), ST_T, 0, s>>>(A, u, r, J);
+  return cudaGetLastError();
+}
 
 template <typename JT, bool DOJ, bool DOR, bool OVW>
 cudaError_t launch_stored(const mrg_problem* p, const StoredArgs& A, const double* u, double* r, JT* J,
@@ -381,24 +555,24 @@ cudaError_t launch_stored(const mrg_problem* p, const StoredArgs& A, const doubl
 }  // namespace
 
 bool mrg_stored_eligible(int dim, int order, int kind, int points_per_axis, bool affine) {
-  return !affine && dim == 3 && order == 1 && kind == MRG_THERMAL && points_per_axis == 2;
+  return !affine && (dim == 2 || dim == 3) && order == 1 && kind == MRG_THERMAL && points_per_axis == 2;
 }
 
 int mrg_stored_setup(mrg_problem* p, cudaStream_t s) {
   const int64_t nc = p->ncell;
+  const int d = p->g.dim, npe = p->npe, nq = p->nq, nsym = npe * (npe + 1) / 2;  // 36 (hexahedra) or 10
   double* cell_load = nullptr;
-  MRG_CUDA(cudaMallocAsync(&p->d_khat, (size_t)36 * nc * sizeof(double), s));
-  MRG_CUDA(cudaMallocAsync(&p->d_khat32, (size_t)36 * nc * sizeof(float), s));
+  MRG_CUDA(cudaMallocAsync(&p->d_khat, (size_t)nsym * nc * sizeof(double), s));
+  if (d == 3) MRG_CUDA(cudaMallocAsync(&p->d_khat32, (size_t)nsym * nc * sizeof(float), s));  // 2-D: FP64 only
   MRG_CUDA(cudaMallocAsync(&p->d_bload, (size_t)p->ndof * sizeof(double), s));
-  MRG_CUDA(cudaMallocAsync(&cell_load, (size_t)8 * nc * sizeof(double), s));
+  MRG_CUDA(cudaMallocAsync(&cell_load, (size_t)npe * nc * sizeof(double), s));
   GeoArgs A;
   A.g = p->g;
-  const int npe = p->npe, nq = p->nq;
   A.tab.w = p->d_qtab;
   A.tab.phi = A.tab.w + nq;
   A.tab.dphi = A.tab.phi + npe * nq;
-  A.tab.psi = A.tab.dphi + npe * nq * 3;
-  A.tab.dpsi = A.tab.psi + 8 * nq;
+  A.tab.psi = A.tab.dphi + npe * nq * d;
+  A.tab.dpsi = A.tab.psi + npe * nq;
   A.vcoord = p->d_vcoord;
   A.src_sin = (p->source_kind == MRG_SRC_SINPROD);
   A.amp = p->source_amp;
@@ -407,10 +581,12 @@ int mrg_stored_setup(mrg_problem* p, cudaStream_t s) {
   A.khat = p->d_khat;
   A.khat32 = p->d_khat32;
   A.bload = cell_load;
-  k_geo_hex<<<nblk(nc, GEO_CPB), GEO_CPB * 8, 0, s>>>(A);
+  if (d == 3) k_geo_hex<<<nblk(nc, GEO_CPB), GEO_CPB * 8, 0, s>>>(A);
+  else k_geo_quad<<<nblk(nc, GEO2_CPB), GEO2_CPB * 4, 0, s>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
-    k_node_load<<<nblk(p->ndof, 256), 256, 0, s>>>(p->g, p->ndof, nc, cell_load, p->d_bload);
+    if (d == 3) k_node_load<<<nblk(p->ndof, 256), 256, 0, s>>>(p->g, p->ndof, nc, cell_load, p->d_bload);
+    else k_node_load_quad<<<nblk(p->ndof, 256), 256, 0, s>>>(p->g, p->ndof, nc, cell_load, p->d_bload);
     e = cudaGetLastError();
   }
   cudaFreeAsync(cell_load, s);
@@ -430,6 +606,27 @@ int mrg_launch_stored(mrg_problem* p, const double* u, double* r, void* J, uint3
   A.ncell = p->ncell;
   const bool doJ = (flags & MRG_ASM_JAC) && J, doR = (flags & MRG_ASM_RES) && r, ovw = flags & MRG_ASM_OVERWRITE;
   cudaError_t e = cudaSuccess;
+  if (p->g.dim == 2) {
+    // quadrilaterals: one launch per pass (k_stored_quad)
+    if (doJ && (flags & MRG_ASM_J_FP32)) {
+      float* J32 = (float*)J;
+      e = doR ? (ovw ? launch_stored_quad<float, true, true, true>(p, A, u, r, J32, s)
+                     : launch_stored_quad<float, true, true, false>(p, A, u, r, J32, s))
+              : (ovw ? launch_stored_quad<float, true, false, true>(p, A, u, nullptr, J32, s)
+                     : launch_stored_quad<float, true, false, false>(p, A, u, nullptr, J32, s));
+    } else if (doJ) {
+      double* J64 = (double*)J;
+      e = doR ? (ovw ? launch_stored_quad<double, true, true, true>(p, A, u, r, J64, s)
+                     : launch_stored_quad<double, true, true, false>(p, A, u, r, J64, s))
+              : (ovw ? launch_stored_quad<double, true, false, true>(p, A, u, nullptr, J64, s)
+                     : launch_stored_quad<double, true, false, false>(p, A, u, nullptr, J64, s));
+    } else if (doR) {
+      e = ovw ? launch_stored_quad<double, false, true, true>(p, A, u, r, nullptr, s)
+              : launch_stored_quad<double, false, true, false>(p, A, u, r, nullptr, s);
+    }
+    if (e != cudaSuccess) return mrg_cuda_check(e, "stored-geometry assembly launch");
+    return MRG_OK;
+  }
   if (doJ && (flags & MRG_ASM_J_FP32)) {
     // mixed: the FP32 Jacobian pass, then (below) the FP64 residual pass: one fused launch holds both rows
     // and both copies of the stored stiffness and measured slower than the two

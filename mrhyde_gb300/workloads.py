@@ -42,25 +42,35 @@ def c2(seed: int = 2, n: int = 128):
 
 
 def perturbed_vertices(n, amp: float = 0.2, seed: int = 12, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0)):
-    """Vertex coordinates [(nx+1)(ny+1)(nz+1), 3] (x fastest) of a box whose interior vertices are moved by
-    up to amp * h per axis (uniform, seeded): non-affine hexahedra, the general per-cell path."""
+    """Vertex coordinates [prod(n_k + 1), len(n)] (x fastest) of a box of len(n) = 2 or 3 axes whose
+    interior vertices are moved by up to amp * h per axis (uniform, seeded): non-affine quadrilaterals or
+    hexahedra, the general geometry paths."""
+    d = len(n)
     rng = np.random.default_rng(seed)
-    axes = [np.linspace(lo[k], hi[k], n[k] + 1) for k in range(3)]
-    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
-    pts = np.stack([x.reshape(-1), y.reshape(-1), z.reshape(-1)], axis=1)
-    iz, iy, ix = np.meshgrid(*[np.arange(n[k] + 1) for k in (2, 1, 0)], indexing="ij")
-    idx = np.stack([ix.reshape(-1), iy.reshape(-1), iz.reshape(-1)], axis=1)
+    axes = [np.linspace(lo[k], hi[k], n[k] + 1) for k in range(d)]
+    grids = np.meshgrid(*reversed(axes), indexing="ij")  # slowest axis first
+    pts = np.stack([grids[d - 1 - k].reshape(-1) for k in range(d)], axis=1)
+    idx_grids = np.meshgrid(*[np.arange(n[k] + 1) for k in reversed(range(d))], indexing="ij")
+    idx = np.stack([idx_grids[d - 1 - k].reshape(-1) for k in range(d)], axis=1)
     interior = np.all((idx > 0) & (idx < np.array(n)), axis=1)
-    h = np.array([(hi[k] - lo[k]) / n[k] for k in range(3)])
-    pts[interior] += amp * h * rng.uniform(-1.0, 1.0, (int(interior.sum()), 3))
+    h = np.array([(hi[k] - lo[k]) / n[k] for k in range(d)])
+    pts[interior] += amp * h * rng.uniform(-1.0, 1.0, (int(interior.sum()), d))
     return np.ascontiguousarray(pts)
 
 
 def c2_general(seed: int = 2, n: int = 128, amp: float = 0.2):
     """C2 on a mesh of non-affine hexahedra (interior vertices perturbed by up to 0.2 h): the same
-    coefficients, source and boundary data as C2, assembled by the general per-cell path."""
+    coefficients, source and boundary data as C2, assembled by the general geometry path."""
     cfg = c2(seed=seed, n=n)
     cfg["vertex_coords"] = perturbed_vertices((n, n, n), amp, seed + 10)
+    return cfg
+
+
+def c1_general(seed: int = 1, n: int = 2048, amp: float = 0.2):
+    """C1's coefficients, source and boundary data on n^2 non-affine quadrilaterals (interior vertices
+    perturbed by up to 0.2 h)."""
+    cfg = c1(seed=seed, n=n)
+    cfg["vertex_coords"] = perturbed_vertices((n, n), amp, seed + 10, lo=(0.0, 0.0), hi=(1.0, 1.0))
     return cfg
 
 

@@ -4,7 +4,10 @@ must return exactly the bits of the FP64 operations they replace:
 * fix_to_f64_bits(s, emax): a 64-bit fixed-point kappa sum rounded once to FP64 (nearest, ties to even),
   against the exact value s * 2^(emax - 1082) held in a long double (64-bit or wider significand) and
   rounded by the conversion to double;
-* mul_bits(mk, ms, ek + es): the product of two normal doubles, against the IEEE multiply.
+* mul_bits(mk, ms, ek + es): the product of two normal doubles, against the IEEE multiply;
+* f64_to_f32_bits(b): an FP64 value rounded to FP32 (nearest, ties to even), against the host's
+  conversion, over FP32's whole normal range, ties, carries into the exponent and overflow to infinity,
+  and declining (for the conversion instruction) exactly outside that range.
 
 The header's device functions compile as plain C++ here; the checker is built with the host compiler and
 runs a few million random and structured cases in about a second.
@@ -75,6 +78,34 @@ int main() {
         for (int eb = 900; eb < 1150; eb += 11) mul(((uint64_t)ea << 52) | pa, ((uint64_t)eb << 52) | pb);
   for (long i = 0; i < 1000000; ++i)  // 2- and 3-bit significands: exact products and ties
     mul((1023ull << 52) | (g() & 0xfffffffffffffull), (1023ull << 52) | ((g() & 0x3ull) << 50));
+  // ---- f64_to_f32_bits
+  auto cvt = [&](uint64_t b) {
+    const int e = (int)((b >> 52) & 0x7ff);
+    uint32_t f = 0;
+    const bool ok = mrgfix::f64_to_f32_bits(b, f);
+    ++tot;
+    if (ok != (e >= 897 && e <= 1150)) {
+      if (bad < 5) std::printf("cvt range: %a\n", dbl(b));
+      ++bad;
+      return;
+    }
+    if (!ok) return;
+    const float want = (float)dbl(b);
+    uint32_t wb;
+    std::memcpy(&wb, &want, 4);
+    if (f != wb) {
+      if (bad < 5) std::printf("cvt: %a -> %08x want %08x\n", dbl(b), f, wb);
+      ++bad;
+    }
+  };
+  for (long i = 0; i < 3000000; ++i)
+    cvt(((g() & 1) << 63) | ((uint64_t)(880 + g() % 290) << 52) | (g() & 0xfffffffffffffull));
+  // the 29 dropped bits at and around the tie, odd and even kept significands, all-ones carries
+  const uint64_t low[] = {0, 1, 0x0fffffff, 0x10000000, 0x10000001, 0x1fffffff, 0x30000000, 0x20000000};
+  for (int e = 890; e <= 1160; ++e)
+    for (uint64_t lw : low)
+      for (uint64_t top : {0ull, 1ull, 2ull, 3ull, 0x7ffffeull, 0x7fffffull, 0x400000ull})
+        for (uint64_t sgn : {0ull, 1ull}) cvt((sgn << 63) | ((uint64_t)e << 52) | (top << 29) | lw);
   std::printf("%ld %ld\n", tot, bad);
   return bad != 0;
 }
@@ -92,4 +123,4 @@ def test_integer_fp64_helpers_match_fp64_operations(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     tot, bad = map(int, out.stdout.split()[-2:])
     assert out.returncode == 0 and bad == 0, out.stdout
-    assert tot > 4_000_000
+    assert tot > 7_000_000

@@ -102,8 +102,9 @@ def test_per_cell_ad_path_general_geometry_and_physics(cuda, i, atomic):
     u = rng.uniform(0.0, 0.5, O.ndof)
     ro, Jo = O.assemble(u)
     G, r, J = _run(cfg, u, atomic=atomic)
-    # thermal Q1 hexahedra take the stored-geometry row gather unless the atomic AD scatter is asked for
-    stored = dim == 3 and cfg["order"] == 1 and cfg["kind"] == "thermal"
+    # thermal Q1 cells (quadrilaterals and hexahedra) take the stored-geometry row gather unless the atomic
+    # AD scatter is asked for
+    stored = cfg["order"] == 1 and cfg["kind"] == "thermal"
     assert G.info.path == (4 if stored else 2)
     assert scaled_err(J, Jo) <= TOL64
     assert scaled_err(r, ro) <= TOL64

@@ -1,4 +1,5 @@
-"""Thermal assembly on general (non-affine) Q1 hexahedra from per-cell geometry stored at creation.
+"""Thermal assembly on general (non-affine) Q1 hexahedra and quadrilaterals from per-cell geometry stored
+at creation.
 
 Checked against the oracle's forward-AD assembly on the same vertex coordinates and against the per-cell
 AD kernels of the library (MRG_ASM_FORCE_CELL): FP64 Jacobian 1e-12 per entry (floor 1e-3 of the
@@ -19,16 +20,22 @@ CASES = [
     dict(n=(7, 2, 5), lo=(0.0, 0.0, 0.0), hi=(0.7, 0.2, 0.5), faces=16 | 2, source=("const", -2.0, 0.0), amp=0.2),
     dict(n=(1, 1, 1), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), faces=0, source=("const", 1.0, 0.0), amp=0.0),
     dict(n=(24, 20, 16), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), faces=3, source=("sinprod", 1.0, 3.0), amp=0.25),
+    # quadrilaterals
+    dict(n=(5, 4), lo=(0.0, 0.0), hi=(1.0, 1.0), faces=1 | 4, source=("sinprod", 2.0, 1.5), amp=0.25),
+    dict(n=(3, 7), lo=(-1.0, 0.5), hi=(2.0, 1.0), faces=15, source=("const", -1.0, 0.0), amp=0.3),
+    dict(n=(1, 1), lo=(0.0, 0.0), hi=(1.0, 1.0), faces=0, source=("const", 1.0, 0.0), amp=0.0),
+    dict(n=(90, 70), lo=(0.0, 0.0), hi=(1.0, 0.6), faces=2, source=("sinprod", 1.0, 3.0), amp=0.25),
 ]
 
 
 def _cfg(i):
     c = CASES[i]
+    dim = len(c["n"])
     rng = np.random.default_rng(300 + i)
-    return dict(dim=3, order=1, n=c["n"], lo=c["lo"], hi=c["hi"], kind="thermal", source=c["source"],
+    return dict(dim=dim, order=1, n=c["n"], lo=c["lo"], hi=c["hi"], kind="thermal", source=c["source"],
                 kappa=np.exp(0.5 * rng.standard_normal(int(np.prod(c["n"])))), dirichlet_faces=c["faces"],
                 dirichlet=("const", 0.25),
-                vertex_coords=perturbed_vertices(3, c["n"], c["lo"], c["hi"], c["amp"], 310 + i))
+                vertex_coords=perturbed_vertices(dim, c["n"], c["lo"], c["hi"], c["amp"], 310 + i))
 
 
 def _oracle(cfg, u):
@@ -63,24 +70,28 @@ def test_stored_geometry_matches_oracle(cuda, i):
     A.assembleJacRes(ud, r2, J2, force_cell=True)
     assert scaled_err(Jn, J2.cpu().numpy()) <= TOL64
     assert term_rel_err(rn, r2.cpu().numpy(), s) <= TOL64
-    # mixed precision: FP32 Jacobian; its FP64 residual is the residual-only pass's, bit for bit
+    # mixed precision: FP32 Jacobian.  Its FP64 residual is, bit for bit, the residual-only pass's on
+    # hexahedra (the mixed pass runs it) and the FP64 pass's on quadrilaterals (the same FP64 row, b - J u)
     r3, J3 = G.new_vector(), G.new_matrix_values(fp32=True)
     J3.fill_(np.nan)
     A.assembleJacRes(ud, r3, J3, fp32_jacobian=True, overwrite=True)
     assert scaled_err(J3.cpu().numpy(), Jo) <= TOL32
     r4 = G.new_vector()
     A.assembleRes(ud, r4, overwrite=True)
-    assert torch.equal(r3, r4)
+    assert torch.equal(r3, r4 if cfg["dim"] == 3 else r)
     assert term_rel_err(r4.cpu().numpy(), ro, s) <= TOL64
+    if cfg["dim"] == 2:  # on quadrilaterals the FP32 Jacobian is the FP64 one rounded once
+        assert torch.equal(J3, J.float())
 
 
 @pytest.mark.gpu
-def test_stored_geometry_passes_agree_and_sum_into(cuda):
+@pytest.mark.parametrize("i", [0, 6])
+def test_stored_geometry_passes_agree_and_sum_into(cuda, i):
     import scipy.sparse as sp
 
     from mrhyde_gb300 import AssemblyManager
 
-    cfg = _cfg(0)
+    cfg = _cfg(i)
     G = gpu_problem(cfg)
     A = AssemblyManager(G)
     ud = torch.tensor(np.random.default_rng(5).uniform(-1, 1, G.info.n_dofs), device="cuda")
@@ -127,11 +138,12 @@ def test_stored_geometry_passes_agree_and_sum_into(cuda):
 
 
 @pytest.mark.gpu
-def test_stored_geometry_follows_new_kappa(cuda):
+@pytest.mark.parametrize("i", [2, 5])
+def test_stored_geometry_follows_new_kappa(cuda, i):
     """The stored data is kappa-free: set_kappa after creation changes J and r as in the oracle."""
     from mrhyde_gb300 import AssemblyManager
 
-    cfg = _cfg(2)
+    cfg = _cfg(i)
     G = gpu_problem(cfg)
     kap2 = np.exp(np.random.default_rng(9).standard_normal(G.info.n_cells))
     G.set_kappa(torch.tensor(kap2, device="cuda"))
@@ -146,12 +158,16 @@ def test_stored_geometry_follows_new_kappa(cuda):
 
 
 @pytest.mark.gpu
-def test_stored_geometry_newton_matches_oracle(cuda):
-    """Newton (a linear problem: one step) with Jacobi PCG on a perturbed 12^3 mesh, FP64 and mixed."""
+@pytest.mark.parametrize("dim", [2, 3])
+def test_stored_geometry_newton_matches_oracle(cuda, dim):
+    """Newton (a linear problem: one step) with Jacobi PCG on a perturbed 12^3 or 40^2 mesh, FP64 and mixed."""
     from mrhyde_gb300 import SolverManager
 
-    cfg = dict(_cfg(0), n=(12, 12, 12), kappa=np.exp(0.5 * np.random.default_rng(4).standard_normal(12 ** 3)),
-               vertex_coords=perturbed_vertices(3, (12, 12, 12), (0, 0, 0), (1, 1, 1), 0.25, 44))
+    n = (12, 12, 12) if dim == 3 else (40, 40)
+    ncell = int(np.prod(n))
+    cfg = dict(_cfg(0 if dim == 3 else 5), n=n, lo=(0.0,) * dim, hi=(1.0,) * dim,
+               kappa=np.exp(0.5 * np.random.default_rng(4).standard_normal(ncell)),
+               vertex_coords=perturbed_vertices(dim, n, (0, 0, 0), (1, 1, 1), 0.25, 44))
     O = oracle_problem(cfg)
     uo = O.set_dirichlet(np.zeros(O.ndof))
     uo, rc, _ = O.newton(uo, nltol=1e-10, maxiter=10, lintol=1e-13)
