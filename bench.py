@@ -53,10 +53,11 @@ def read_peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the headline kernel,
 # k_fact_hex<double,1,1,1,1>, on the 128^3 workload, from one ncu capture of
-#     ncu --set full --clock-control none -k regex:k_fact_hex -s 1 -c 1 -o fact_hex_fp64 \
-#         python bench.py --profile fp64 --steps 2 --warmup 1
+#     ncu --set full --clock-control none -k regex:k_fact_hex -s 2 -c 1 -o fact_hex_fp64 \
+#         python bench.py --profile fp64 --steps 3 --warmup 2
+# (k_kappa_scale, the other launch of the assembly call, moves 33.6 MB more)
 # (this run does not measure it; the bench line says so next to the value)
-C2_FP64_DRAM_BYTES_CAPTURED = 449_116_672
+C2_FP64_DRAM_BYTES_CAPTURED = 448_142_336
 
 
 class ClockSampler:
@@ -308,9 +309,10 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": WORKLOAD, "cells": cells, "dofs": info.n_dofs, "nnz": info.nnz,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed before every timed step (256 MB write, outside the step's CUDA events)",
-                   "path": "factored row-gather (kappa_c * K_ref, one CSR row per thread, smem-staged 16B stores; "
-                            "kappa sums exact in 64-bit fixed point, rounded once to FP64; FP64 products and residual; "
-                            "the axis-neighbour entries of cubic cells (coefficient +0) without FP64 instructions)"},
+                   "path": "factored row-gather (kappa_c * K_ref, one CSR row per thread, smem-staged 16B stores); "
+                            "cubic cells: k_kappa_scale forms |K| kappa_c per cell, then every entry is the exact "
+                            "64-bit fixed-point sum of its cells' scaled conductances rounded once (no FP64 "
+                            "instruction), axis-neighbour entries +0, residual 21 FP64 FMAs per row"},
         "dof_per_s": world * info.n_dofs * args.steps / (tot64 * 1e-3),
         "mixed": {"value": world * cells * args.steps / (tot32 * 1e-3), "unit": "cells/s",
                   "ms_per_step": tot32 / args.steps, "dtype": "J f32 / residual f64",
@@ -322,6 +324,7 @@ def run_ours(args, rank, world, local_rank):
                      "traffic_source": "ncu capture of one launch of this kernel on this workload (dram read + write "
                                        "bytes; a constant in bench.py, not measured by this run)",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "duration": "CUDA events around the whole assembly call (k_kappa_scale + k_fact_hex)",
                      "algorithmic_bytes_per_launch": algo64,
                      "fp64_pipe": {"dp_instr_per_launch": dp_ops, "achieved_dp_instr_per_s": dp_ops / (ms_step * 1e-3),
                                    "peak_dp_instr_per_s": dp_peak, "frac": dp_ops / (ms_step * 1e-3) / dp_peak,
@@ -330,7 +333,7 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": world * cells * n_e2e / (tot_e2e * 1e-3), "unit": "cells/s",
                 "h2d_bytes_per_step": info.n_dofs * 8, "d2h_bytes_per_step": info.nnz * 8 + info.n_dofs * 8,
                 "schedule": "two buffer sets on two streams: step k+1's upload and assembly overlap step k's copy-back"},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,  # k_kappa_scale + k_fact_hex per step
     }
     out["mixed"]["roofline_frac"] = algo32 / (tot32 / args.steps * 1e-3) / 1e9 / peaks["hbm_gbs"]
     if sampler:
@@ -650,10 +653,11 @@ def max_over_ranks(x: float, dist=None, device="cpu") -> float:
 
 
 def fp64_instructions(cfg):
-    """FP64 instructions of one FP64 Jac+res launch of the factored Q1 kernel on a box with Dirichlet rows on
-    the x = 0 and x = 1 faces: a DMUL (K(off) * S(off)) and a DFMA (residual) per entry of a free row, except
-    the axis-neighbour entries of cubic cells, whose coefficient is +0 and which take no FP64 instruction.
-    The kappa sums are exact fixed-point sums on the integer pipes (no FP64 instruction)."""
+    """FP64 instructions of one FP64 Jac+res assembly of the factored Q1 path on a box with Dirichlet rows on
+    the x = 0 and x = 1 faces.  Box cells: a DMUL (K(off) * S(off)) and a DFMA (residual) per entry of a free
+    row.  Cubic cells: the axis-neighbour entries take none (K = +0) and the others one DFMA each (the
+    entries are exact sums of scaled conductances, formed on the integer pipes), plus one DMUL per cell in
+    k_kappa_scale.  The kappa sums are exact fixed-point sums on the integer pipes (no FP64 instruction)."""
     import numpy as np
 
     n = [c + 1 for c in cfg["n"]]
@@ -663,6 +667,7 @@ def fp64_instructions(cfg):
     entries = int(((1 + bx) * (1 + by) * (1 + bz)).sum())
     if h[0] == h[1] == h[2]:
         entries -= int((bx + by + bz).sum())
+        return entries + int(np.prod(cfg["n"]))
     return 2 * entries
 
 

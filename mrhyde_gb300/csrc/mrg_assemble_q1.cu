@@ -14,6 +14,11 @@
 //      and forms r_i = b_i - sum_off J(i,i+off) u(i+off).  Rows of one CTA are contiguous in CSR, so
 //      the CTA stages its segment in shared memory and writes it with 16-byte streaming stores.  No
 //      atomics, no column search, no zero-fill pass, every nonzero written exactly once.
+//      Cubic cells: K is +0 on the 6 axis offsets and one value -|K| on the other 20 (diagonal 4 |K|), so
+//      the products fold into the conductances: k_kappa_scale forms |K| kappa_c once per cell, and each
+//      entry is the exact fixed-point sum of its cells' scaled conductances rounded once (diagonal: times
+//      4, an exponent shift), with the sign set on the integer pipe.  The only FP64 instructions of a row
+//      are then the residual's 21 FMAs (42 with the products).
 //
 //  (2) Per-cell path (any geometry; any physics form; Q1 or Q2).  One CTA slice per cell: one
 //      thread per quadrature point computes the geometric Jacobian from the cell vertices, the
@@ -26,6 +31,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "mrg_device.cuh"
 #include "mrg_fixmul.cuh"
@@ -59,6 +65,14 @@ __device__ __forceinline__ bool nonfinite(double v) {
   return ((unsigned)__double2hiint(v) & 0x7ff00000u) == 0x7ff00000u;
 }
 
+// -v by flipping the sign bit on the integer pipe.  The flip is inline PTX: written in C++, the compiler
+// recognises it as a floating negation and, for a value that is stored, issues it as an FP64 add.
+__device__ __forceinline__ double neg_int(double v) {
+  int hi = __double2hiint(v);
+  asm("xor.b32 %0, %0, 0x80000000;" : "+r"(hi));
+  return __hiloint2double(hi, __double2loint(v));
+}
+
 using mrgdev::row_ptr_of;
 using mrgdev::seg_store;
 
@@ -83,16 +97,18 @@ struct FactArgs {
 // ------------------------------------------------------------------------------------------------
 // (1) factored row-gather, hexahedra.  JT = double (FP64 mode) or float (mixed mode).
 // ------------------------------------------------------------------------------------------------
-// Occupancy floors chosen by measurement: FP64 Jacobians 6 CTAs per SM (80 registers; 0.266 -> 0.253 ms on
-// C2 when introduced; 7 and 8 CTAs, i.e. 72 and 64 registers, spilled more and were slower), FP32 Jacobians
-// 5 (96 registers; 0.252 -> 0.232 ms against the compiler's 117).  The interior-row path of the Jacobian
-// instances spills a few words at this floor and is still faster (FP64 0.201 -> 0.1996 ms, mixed
-// 0.189 -> 0.165 ms).  Residual-only instances (no staged row in shared memory): 8 CTAs per SM, 64
-// registers with spills, 0.167 -> 0.156 ms (7 CTAs: 0.158 ms).
+// Occupancy floors chosen by measurement.  Box cells (products K(off) * S(off)): FP64 Jacobians 6 CTAs per
+// SM (80 registers; 0.266 -> 0.253 ms on C2 when introduced; 7 and 8 CTAs, i.e. 72 and 64 registers,
+// spilled more and were slower), FP32 Jacobians 5 (96 registers; 0.252 -> 0.232 ms against the compiler's
+// 117); the interior-row path spills a few words at these floors and is still faster.  Cubic cells (ZAX:
+// sums of scaled conductances, no products) need fewer registers: FP64 7 CTAs (0.1655 -> 0.1640 ms on C2;
+// 8: 0.172 ms), FP32 6 (0.1685 -> 0.1604 ms).  Residual-only instances (no staged row in shared memory):
+// 8 CTAs per SM, 64 registers with spills, 0.167 -> 0.156 ms on box-cell products (7 CTAs: 0.158 ms).
 template <typename JT, bool DOJ, bool DOR, bool OVW, bool ZAX>
-__global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? 6 : 5)) k_fact_hex(const FactArgs A, const double* __restrict__ u,
-                                                  const double* __restrict__ kap, const float* __restrict__ kap32,
-                                                  double* __restrict__ r, JT* __restrict__ J) {
+__global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 7 : 6) : (ZAX ? 6 : 5)))
+    k_fact_hex(const FactArgs A, const double* __restrict__ u, const double* __restrict__ kap,
+               const double* __restrict__ kraw, const float* __restrict__ kap32, double* __restrict__ r,
+               JT* __restrict__ J) {
   constexpr bool MIXED = sizeof(JT) == 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int64_t s_seg[2];
@@ -176,7 +192,8 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? 6 : 5)) k_fa
               emax = max(emax, e & 0x7ff);
             }
           }
-      fx = fx && emax >= 60 && emax <= 2042;  // rounded sums are normal, finite numbers
+      // rounded sums are normal, finite numbers (ZAX: the diagonal's sum times 4 as well)
+      fx = fx && emax >= 60 && emax <= (ZAX ? 2040 : 2042);
       // S[dz][dy][dx] = sum of kappa over the cells shared by node and node+off
       double S[3][3][3];
       if (fx) {
@@ -225,19 +242,30 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? 6 : 5)) k_fa
                 S[z][y][x] = 0.0;
               } else {
                 const uint64_t q = (z == 0) ? qxy[0][y][x] : (z == 2 ? qxy[1][y][x] : qxy[0][y][x] + qxy[1][y][x]);
-                S[z][y][x] = __longlong_as_double((long long)mrgfix::fix_to_f64_bits(q, emax));
+                // ZAX: the diagonal is 4 |K| S(0) -- a power-of-two scaling of the rounded sum
+                const int es = (ZAX && z == 1 && y == 1 && x == 1) ? emax + 2 : emax;
+                S[z][y][x] = __longlong_as_double((long long)mrgfix::fix_to_f64_bits(q, es));
               }
             }
       }
       if (!fx) {
-        // FP64 additions (rows the fixed point does not cover, or MRG_ASM_NATIVE_FP64)
+        // FP64 additions (rows the fixed point does not cover, or MRG_ASM_NATIVE_FP64) of the cells' own
+        // kappa (ZAX: kap holds the scaled values, so they are read again from kraw)
         double k[2][2][2];
 #pragma unroll
         for (int c = 0; c < 2; ++c)
 #pragma unroll
           for (int b = 0; b < 2; ++b)
 #pragma unroll
-            for (int a = 0; a < 2; ++a) k[c][b][a] = __longlong_as_double((long long)kb[c][b][a]);
+            for (int a = 0; a < 2; ++a) {
+              if (ZAX) {
+                const int ccx = ix - 1 + a, ccy = iy - 1 + b, ccz = iz - 1 + c;
+                const bool ok = ccx >= 0 && ccx < nx && ccy >= 0 && ccy < ny && ccz >= 0 && ccz < nz;
+                k[c][b][a] = ok ? __ldg(kraw + ccx + (int64_t)nx * (ccy + (int64_t)ny * ccz)) : 0.0;
+              } else {
+                k[c][b][a] = __longlong_as_double((long long)kb[c][b][a]);
+              }
+            }
         double sx[2][2][3], sxy[2][3][3];
 #pragma unroll
         for (int c = 0; c < 2; ++c)
@@ -308,78 +336,103 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? 6 : 5)) k_fa
       // FP64 multiply), taking 8 of an interior row's FP64 instructions off the FP64 pipe.  Residual-only
       // instances only (C2: 0.182 -> 0.166 ms); with the Jacobian the register budget is full and the
       // launch measured 2 % slower.
-      const bool icorner = !MIXED && !DOJ && A.kc_ok && fx && A.kc_e + emax - 1030 >= 2 && A.kc_e + emax - 1022 <= 2044;
-      // entry (dz, dy, dx) at position pos of the row
-      auto entry = [&](const int dz, const int dy, const int dx, const int pos) {
-        const int cls = (dx != 0) + 2 * (dy != 0) + 4 * (dz != 0);
-        const double s = S[dz + 1][dy + 1][dx + 1];
-        if (!MIXED) {
-          if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
-            // K = +0: the product +0 * s is a zero with the sign of s (NaN for a non-finite s), and the
-            // residual term -(+-0) * u leaves acc unchanged unless s or u is not finite (then NaN).  No FP64
-            // instruction: on cubic cells 12 of an interior row's 54.
-            const bool sbad = nonfinite(s);
-            if (DOJ)
-              sv[loc + pos] = (JT)__longlong_as_double(
-                  sbad ? 0x7fffffffffffffffll : (long long)((unsigned long long)__double_as_longlong(s) & 0x8000000000000000ull));
-            if (DOR) ubad |= sbad | nonfinite(__ldg(u + n + dx + (int64_t)NX * dy + plane * dz));
+      const bool icorner = !ZAX && !MIXED && !DOJ && A.kc_ok && fx && A.kc_e + emax - 1030 >= 2 && A.kc_e + emax - 1022 <= 2044;
+      // ZAX rows with exact sums: S holds the sums of the scaled conductances |K| kappa (kap), rounded once,
+      // and the entry is -S (diagonal: +4 |K| S(0), already scaled): no FP64 instruction (row_loop below)
+      // The row's entries: SC (ZAX rows with exact sums) takes them from the scaled sums, the other rows
+      // from the products; two compiled copies of the row loop, so that neither carries the other's work
+      auto row_loop = [&](auto sc_tag) {
+        constexpr bool SC = decltype(sc_tag)::value;
+        // entry (dz, dy, dx) at position pos of the row
+        auto entry = [&](const int dz, const int dy, const int dx, const int pos) {
+          const int cls = (dx != 0) + 2 * (dy != 0) + 4 * (dz != 0);
+          const double s = S[dz + 1][dy + 1][dx + 1];
+          if (!MIXED) {
+            if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
+              // K = +0: the product +0 * s is a zero with the sign of s (NaN for a non-finite s), and the
+              // residual term -(+-0) * u leaves acc unchanged unless s or u is not finite (then NaN).  No
+              // FP64 instruction: on cubic cells 12 of an interior row's 54.
+              const bool sbad = nonfinite(s);
+              if (DOJ)
+                sv[loc + pos] = (JT)__longlong_as_double(
+                    sbad ? 0x7fffffffffffffffll : (long long)((unsigned long long)__double_as_longlong(s) & 0x8000000000000000ull));
+              if (DOR) ubad |= sbad | nonfinite(__ldg(u + n + dx + (int64_t)NX * dy + plane * dz));
+            } else if (SC) {
+              // entry s (diagonal) or -s (sign flipped on the integer pipes); residual term -a u with the
+              // negation folded into the FMA
+              if (DOJ)
+                sv[loc + pos] = (JT)(cls == 0 ? s : neg_int(s));
+              if (DOR) acc = fma(cls == 0 ? -s : s, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+            } else {
+              double a;
+              if (cls == 7 && icorner) {
+                const uint64_t sb = (uint64_t)__double_as_longlong(s);  // kappa >= 0
+                a = __longlong_as_double((long long)(A.kc_sign |
+                                                     (sb ? mrgfix::mul_bits(A.kc_m, (sb & 0xfffffffffffffull) | (1ull << 52),
+                                                                            A.kc_e + (int)(sb >> 52))
+                                                         : 0ull)));
+              } else {
+                a = A.Kp[cls] * s;
+              }
+              if (DOJ) sv[loc + pos] = (JT)a;
+              if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+            }
           } else {
-            double a;
-            if (cls == 7 && icorner) {
-              const uint64_t sb = (uint64_t)__double_as_longlong(s);  // kappa >= 0
-              a = __longlong_as_double((long long)(A.kc_sign |
-                                                   (sb ? mrgfix::mul_bits(A.kc_m, (sb & 0xfffffffffffffull) | (1ull << 52),
-                                                                          A.kc_e + (int)(sb >> 52))
-                                                       : 0ull)));
-            } else {
-              a = A.Kp[cls] * s;
+            if (DOJ) {
+              if (cls == 0) {
+                dpos = pos;
+              } else {
+                const float v = A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1];
+                sv[loc + pos] = (JT)v;
+                neumaier_add(osum, ocomp, v);
+              }
             }
-            if (DOJ) sv[loc + pos] = (JT)a;
-            if (DOR) acc = fma(-a, __ldg(u + n + dx + (int64_t)NX * dy + plane * dz), acc);
+            if (DOR) {
+              const double uv = __ldg(u + n + dx + (int64_t)NX * dy + plane * dz);
+              // K = +0 class: K * t is +0 unless S or u is not finite (the same rule as FP64 above)
+              if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
+                ubad |= nonfinite(s) | nonfinite(uv);
+              } else if (SC) {
+                acc = fma(cls == 0 ? -s : s, uv, acc);  // the FP64 pass's entries, one FMA each
+              } else if (ZAX) {
+                acc = fma(-(A.Kp[cls] * s), uv, acc);
+              } else {
+                t[cls] = fma(s, uv, t[cls]);
+              }
+            }
           }
+        };
+        if (DOJ && cx == 3 && cy == 3 && cz == 3) {
+          // interior row: all 27 entries, their positions in the staged row known at compile time (the
+          // residual-only instances keep the single loop: there it measured 5 % slower)
+#pragma unroll
+          for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+              for (int dx = -1; dx <= 1; ++dx) entry(dz, dy, dx, (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
         } else {
-          if (DOJ) {
-            if (cls == 0) {
-              dpos = pos;
-            } else {
-              const float v = A.Kp32[cls] * S32[dz + 1][dy + 1][dx + 1];
-              sv[loc + pos] = (JT)v;
-              neumaier_add(osum, ocomp, v);
-            }
-          }
-          if (DOR) {
-            const double uv = __ldg(u + n + dx + (int64_t)NX * dy + plane * dz);
-            // K = +0 class: K * t is +0 unless S or u is not finite (the same rule as FP64 above)
-            if (ZAX && (cls == 1 || cls == 2 || cls == 4)) ubad |= nonfinite(s) | nonfinite(uv);
-            else t[cls] = fma(s, uv, t[cls]);
-          }
+          int pos = 0;
+#pragma unroll
+          for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+              for (int dx = -1; dx <= 1; ++dx)
+                if (vz[dz + 1] && vy[dy + 1] && vx[dx + 1]) entry(dz, dy, dx, pos++);
         }
       };
-      if (DOJ && cx == 3 && cy == 3 && cz == 3) {
-        // interior row: all 27 entries, their positions in the staged row known at compile time (the
-        // residual-only instances keep the single loop: there it measured 5 % slower)
-#pragma unroll
-        for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-          for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-            for (int dx = -1; dx <= 1; ++dx) entry(dz, dy, dx, (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
+      if constexpr (ZAX) {
+        if (fx) row_loop(std::true_type{});
+        else row_loop(std::false_type{});
       } else {
-        int pos = 0;
-#pragma unroll
-        for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-          for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-            for (int dx = -1; dx <= 1; ++dx)
-              if (vz[dz + 1] && vy[dy + 1] && vx[dx + 1]) entry(dz, dy, dx, pos++);
+        row_loop(std::false_type{});
       }
       if (MIXED && DOJ) sv[loc + dpos] = (JT)(-(osum + ocomp));
       if (DOR) {
-        if (MIXED) {
+        if (MIXED && !ZAX) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c)
-            if (!(ZAX && (c == 1 || c == 2 || c == 4))) acc = fma(-A.Kp[c], t[c], acc);
+          for (int c = 0; c < 8; ++c) acc = fma(-A.Kp[c], t[c], acc);
         }
         if (ZAX && ubad) acc = __longlong_as_double(0x7fffffffffffffffll);
         if (OVW) r[n] = acc; else r[n] += acc;
@@ -786,6 +839,13 @@ __global__ void k_kappa32(const double* __restrict__ k, float* __restrict__ k32,
   if (i < n) k32[i] = (float)k[i];
 }
 
+// Scaled conductances |K| kappa_c of cubic cells, formed at the start of every assembly that needs the FP64
+// entries (one FP64 multiply per cell instead of 21 per row)
+__global__ void k_kappa_scale(const double* __restrict__ k, double ks, double* __restrict__ out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __dmul_rn(k[i], ks);
+}
+
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 template <typename JT, bool DOJ, bool DOR, bool OVW>
@@ -795,7 +855,14 @@ cudaError_t launch_fact(const mrg_problem* p, const FactArgs& A, const double* u
   if (p->g.dim == 3) {
     auto kern = A.zax ? k_fact_hex<JT, DOJ, DOR, OVW, true> : k_fact_hex<JT, DOJ, DOR, OVW, false>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
+    // cubic cells with FP64 entries: the scaled conductances first (the FP32 Jacobian alone needs none)
+    const bool scaled = A.zax && (sizeof(JT) == 8 || DOR);
+    if (scaled) {
+      k_kappa_scale<<<nblk(p->ncell, 256), 256, 0, s>>>(p->d_kappa, p->kscale, p->d_kappa_s, p->ncell);
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, FT, smem, s>>>(A, u, scaled ? p->d_kappa_s : p->d_kappa, p->d_kappa, p->d_kappa32, r, J);
   } else {
     auto kern = k_fact_quad<JT, DOJ, DOR, OVW>;
     kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
@@ -877,8 +944,9 @@ int mrg_launch_factored(mrg_problem* p, const double* u, double* r, void* J, uin
     A.kc_m = (b7 & 0xfffffffffffffull) | (1ull << 52);
     A.kc_sign = b7 & 0x8000000000000000ull;
   }
-  auto pos0 = [&](int c) { return p->Kp[c] == 0.0 && !std::signbit(p->Kp[c]); };
-  A.zax = (A.fixed && p->g.dim == 3 && pos0(1) && pos0(2) && pos0(4)) ? 1 : 0;  // native: every product a DMUL
+  // cubic cells (axis classes +0, the other off-diagonal classes one coefficient): exact sums of scaled
+  // conductances; native: every product a DMUL
+  A.zax = (A.fixed && p->g.dim == 3 && p->cubic) ? 1 : 0;
   if (A.src_sin) {
     A.B[0] = p->d_srcB;
     A.B[1] = p->d_srcB + p->g.nn[0];

@@ -113,6 +113,11 @@ struct mrg_problem {
   double* d_bload = nullptr;    // [ndof] load vector b_i = sum over the node's cells of int f phi_i
   // host copies of small tables
   double Kp[8];                 // factored path: K(|dx|,|dy|,|dz|) of one cell, kappa = 1
+  // cubic cells of the factored path: the axis classes are +0 and the other off-diagonal classes share
+  // one coefficient -|K| (diagonal 4 |K|); d_kappa_s holds |K| kappa_c, formed per assembly
+  int cubic = 0;
+  double kscale = 0.0;
+  double* d_kappa_s = nullptr;
   double cell_load;             // factored path: int_cell phi_l for one node (vol / 2^dim)
   std::vector<double> qtab_host;
   std::vector<double> gx1, gw1;  // 1-D Gauss rule of the problem

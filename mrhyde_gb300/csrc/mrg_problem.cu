@@ -235,6 +235,7 @@ static void free_problem(mrg_problem* p) {
   cudaFreeAsync(p->d_prefix, s);
   cudaFreeAsync(p->d_kappa, s);
   cudaFreeAsync(p->d_kappa32, s);
+  cudaFreeAsync(p->d_kappa_s, s);
   cudaFreeAsync(p->d_fixed, s);
   cudaFreeAsync(p->d_fixed_vals, s);
   cudaFreeAsync(p->d_vcoord, s);
@@ -455,6 +456,22 @@ static int create_impl(const mrg_mesh_desc* m, const mrg_physics_desc* ph, cudaS
     for (int j = 0; j < nvpe; ++j) kmax = std::max(kmax, std::fabs(P->Kp[j]));
     for (int j = 0; j < nvpe; ++j)
       if (std::fabs(P->Kp[j]) <= 64.0 * 2.220446049250313e-16 * kmax) P->Kp[j] = 0.0;
+    // cubic cells: classes 3, 5, 6 and 7 are -h/12 and the diagonal h/3 in exact arithmetic; their
+    // quadrature values agree to rounding.  The factored kernel then sums scaled conductances
+    // |K7| kappa_c (k_kappa_scale) instead of multiplying every kappa sum by its class coefficient.
+    if (d == 3) {
+      const double k7 = P->Kp[7];
+      auto near = [&](double a, double b) { return std::fabs(a - b) <= 64.0 * 2.220446049250313e-16 * std::fabs(b); };
+      const bool axis0 = P->Kp[1] == 0.0 && P->Kp[2] == 0.0 && P->Kp[4] == 0.0 && !std::signbit(P->Kp[1]) &&
+                         !std::signbit(P->Kp[2]) && !std::signbit(P->Kp[4]);
+      if (axis0 && k7 < 0.0 && std::isnormal(k7) && near(P->Kp[3], k7) && near(P->Kp[5], k7) && near(P->Kp[6], k7) &&
+          near(P->Kp[0], -4.0 * k7)) {
+        P->cubic = 1;
+        P->kscale = -k7;
+        if ((e = cudaMallocAsync(&P->d_kappa_s, P->ncell * sizeof(double), cs)) != cudaSuccess)
+          return fail_cuda(e, "cudaMalloc scaled kappa");
+      }
+    }
     double ld = 0.0;
     for (int q = 0; q < nq; ++q) ld += tphi[0 * nq + q] * tw[q] * detJ;
     P->cell_load = ld;

@@ -1,6 +1,8 @@
-"""Host logic of bench.py's roofline: the FP64 instruction count of the factored Q1 Jacobian+residual launch,
-against a brute-force enumeration of the free rows' entries (a multiply and an FMA per entry, none for the
-axis-neighbour entries of cubic cells, whose coefficient is +0; rows on x = 0 and x = 1 are Dirichlet)."""
+"""Host logic of bench.py's roofline: the FP64 instruction count of the factored Q1 Jacobian+residual
+assembly, against a brute-force enumeration of the free rows' entries (rows on x = 0 and x = 1 are
+Dirichlet).  Box cells: a multiply and an FMA per entry.  Cubic cells: none for the axis-neighbour entries
+(coefficient +0), an FMA for each other entry (the entries are exact sums of scaled conductances) and one
+multiply per cell (the scaling)."""
 import itertools
 
 import pytest
@@ -22,8 +24,8 @@ def _brute(n, hi):
                 continue
             if cubic and (dx != 0) + (dy != 0) + (dz != 0) == 1:
                 continue
-            count += 2
-    return count
+            count += 1 if cubic else 2
+    return count + (n[0] * n[1] * n[2] if cubic else 0)
 
 
 @pytest.mark.parametrize("n,hi", [((4, 4, 4), (1.0, 1.0, 1.0)), ((5, 3, 4), (1.0, 1.0, 1.0)),
