@@ -126,7 +126,10 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 7 : 6
     axis_range(ix, NX, 1, lo, cx);
     axis_range(iy, NY, 1, lo, cy);
     axis_range(iz, NZ, 1, lo, cz);
-    myrow = g.P[2][iz] * g.T[1] * g.T[0] + (int64_t)cz * (g.P[1][iy] * g.T[0] + (int64_t)cy * g.P[0][ix]);
+    // Q1: an axis node couples 2 nodes at either end of the axis and 3 inside, so the prefix of the counts is
+    // P[i] = max(3 i - 1, 0): no table loads ahead of the CTA barrier (C2 0.1638 -> 0.1620 ms)
+    const int64_t px = max(3 * ix - 1, 0), py = max(3 * iy - 1, 0), pz = max(3 * iz - 1, 0);
+    myrow = pz * g.T[1] * g.T[0] + (int64_t)cz * (py * g.T[0] + (int64_t)cy * px);
   }
   // the CTA's CSR segment: from its first row's start to its last row's end (rows are contiguous in CSR)
   int64_t seg0 = 0, seg1 = 0;
