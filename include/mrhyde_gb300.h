@@ -165,7 +165,7 @@ int mrg_get_fixed_dofs(const mrg_problem* p, int32_t* dofs /*[n_fixed]*/, double
 int mrg_set_kappa(mrg_problem* p, const double* kappa_dev /*[n_cells]*/, mrg_stream_t stream);
 int mrg_set_dirichlet(const mrg_problem* p, double* u_dev /*[n_dofs]*/, mrg_stream_t stream);
 
-/* ---- boundary terms on box faces (thermal.cpp:170-260) --------------------------------------- *
+/* ---- boundary terms on mesh faces (thermal.cpp:170-260) -------------------------------------- *
  * Faces are numbered 0..2*dim-1 = x-, x+, y-, y+, z-, z+ (bit f of MRG_FACE_*).  Side points of a face are
  * ordered by face cell (first tangential cell index fastest) and then by point of the cell's side rule
  * (the problem's 1-D Gauss rule on the tangential axes, first tangential axis fastest).
@@ -173,8 +173,10 @@ int mrg_set_dirichlet(const mrg_problem* p, double* u_dev /*[n_dofs]*/, mrg_stre
  *   MRG_BC_WEAK_DIRICHLET  Nitsche terms with penalty 10/h, h = face measure^(1/(dim-1)), form_param 1:
  *                          res_i += 10/h k (u - g) phi_i - k (grad u . n) phi_i - k (u - g) (grad phi_i . n)
  *                          (k = kappa_c, or 1 + u^2), in r (as -res) and in J.
- * Box cells only (no vertex_coords): MRG_ENOTSUP otherwise.  A face with a strong Dirichlet condition
- * cannot also carry one of these (MRG_EINVAL). */
+ * Box cells and general cells (vertex_coords): on general cells each face cell's side weights, outward
+ * normals and h come from its own geometry, computed when the condition is set.  At most 4 points per
+ * axis in the side rule (MRG_ENOTSUP otherwise).  A face with a strong Dirichlet condition cannot also
+ * carry one of these (MRG_EINVAL). */
 enum { MRG_BC_NONE = 0, MRG_BC_NEUMANN = 1, MRG_BC_WEAK_DIRICHLET = 2 };
 /* *npts = number of side points of the face; xyz (host, [npts][3], z = 0 in 2-D) may be NULL. */
 int mrg_get_side_points(const mrg_problem* p, int32_t face, int64_t* npts, double* xyz);

@@ -1,4 +1,6 @@
-"""Face boundary terms on the GPU (Neumann and weakly imposed Dirichlet data) against the oracle.
+"""Face boundary terms on the GPU (Neumann and weakly imposed Dirichlet data) against the oracle, on box
+cells and on general (non-affine) cells, whose side weights, normals and element sizes come from each face
+cell's own geometry.
 
 Reference: thermal::boundaryResidual (src/physics/thermal.cpp:170-260) in the boundary workset loop of
 assembleJacRes (src/managers/assembly/assemblyManager_jacres.hpp:485-603).  Same seeded inputs and the
@@ -40,17 +42,33 @@ def _data(xyz, face):
     return np.sin(1.7 * xyz[:, 0] + 0.3 * face) * np.cos(2.3 * xyz[:, 1]) + 0.25 * xyz[:, 2] + 0.1 * face
 
 
-def _setup(cfg, faces, seed):
+def _moved_vertices(dim, n, lo, hi, amp, seed):
+    """Vertex grid of a box with every vertex moved by up to amp * h per axis: non-affine cells whose
+    boundary faces are neither flat nor axis-aligned (side measures and normals differ per face cell)."""
+    rng = np.random.default_rng(seed)
+    axes = [np.linspace(lo[k], hi[k], n[k] + 1) for k in range(dim)]
+    grids = np.meshgrid(*reversed(axes), indexing="ij")  # slowest axis first
+    pts = np.stack([grids[dim - 1 - k].reshape(-1) for k in range(dim)], axis=1)
+    h = np.array([(hi[k] - lo[k]) / n[k] for k in range(dim)])
+    pts += amp * h * rng.uniform(-1, 1, pts.shape)
+    return np.ascontiguousarray(pts)
+
+
+def _setup(cfg, faces, seed, general=False):
     rng = np.random.default_rng(seed)
     ncell = int(np.prod(cfg["n"]))
     c = dict(cfg)
     if c.get("kind", "thermal") == "thermal":
         c["kappa"] = np.exp(0.5 * rng.standard_normal(ncell))
+    if general:
+        lo = c.get("lo", (0.0, 0.0, 0.0))
+        hi = c.get("hi", (1.0, 1.0, 1.0))
+        c["vertex_coords"] = _moved_vertices(c["dim"], c["n"], lo, hi, 0.2, seed + 100)
     G, O = gpu_problem(c), oracle_problem(c)
     for face, kind in faces.items():
         xo = O.side_points(face)
         xg = G.side_points(face)
-        np.testing.assert_allclose(xg, xo, rtol=0, atol=1e-14)
+        np.testing.assert_allclose(xg, xo, rtol=0, atol=1e-13)
         g = _data(xo, face)
         O.set_face_bc(face, ORC_KIND[kind], g)
         G.set_face_bc(face, kind, g)
@@ -79,6 +97,40 @@ def test_face_terms_match_oracle(cuda, case, fp32):
     A.assembleRes(ud, r2, overwrite=True)
     torch.cuda.synchronize()
     assert scaled_err(r2.cpu().numpy(), ro) <= TOL64
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+@pytest.mark.parametrize("fp32", [False, True])
+def test_face_terms_general_geometry_match_oracle(cuda, case, fp32):
+    """Perturbed interior vertices: the volume terms take the stored-geometry or the per-cell AD path, the
+    face terms each face cell's own weights, normal derivatives and element size."""
+    from mrhyde_gb300 import AssemblyManager
+
+    cfg, faces, tol32 = case
+    G, O, u = _setup(cfg, faces, 7, general=True)
+    ro, Jo = O.assemble(u)
+    A = AssemblyManager(G)
+    ud = torch.tensor(u, device="cuda")
+    r, J = G.new_vector(), G.new_matrix_values(fp32=fp32)
+    A.assembleJacRes(ud, r, J, fp32_jacobian=fp32, overwrite=True)
+    torch.cuda.synchronize()
+    assert scaled_err(r.cpu().numpy(), ro) <= TOL64
+    # FP32: the stored-geometry Jacobian forms its products in FP32 and the face terms add one more FP32
+    # rounding, each relative to terms that cancel on distorted cells (measured at most 4.0e-6 over the
+    # cases, box cells up to 3.7e-5)
+    assert scaled_err(J.cpu().numpy(), Jo) <= (max(tol32, 1e-5) if fp32 else TOL64)
+    r2 = G.new_vector()
+    A.assembleRes(ud, r2, overwrite=True)
+    torch.cuda.synchronize()
+    assert scaled_err(r2.cpu().numpy(), ro) <= TOL64
+    # the boundary terms are there: without them the residual differs
+    for face in faces:
+        G.set_face_bc(face, "none")
+    r3 = G.new_vector()
+    A.assembleRes(ud, r3, overwrite=True)
+    torch.cuda.synchronize()
+    assert scaled_err(r3.cpu().numpy(), ro) > 1e-6
 
 
 @pytest.mark.gpu
@@ -111,7 +163,9 @@ def test_face_bc_argument_checks(cuda):
     H = gpu_problem(dict(dim=2, order=1, n=(3, 3), dirichlet_faces=1,
                          vertex_coords=perturbed_vertices(2, (3, 3), (0, 0, 0), (1, 1, 1), 0.1, 2)))
     with pytest.raises(MrgError):
-        H.set_face_bc(1, "neumann")          # non-affine cells are not supported on the device
+        H.set_face_bc(0, "weak_dirichlet")   # strong Dirichlet face, non-affine cells
+    H.set_face_bc(1, "neumann")              # non-affine cells: per-cell side geometry
+    H.set_face_bc(1, "none")
 
 
 @pytest.mark.gpu
