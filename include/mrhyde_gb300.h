@@ -186,6 +186,10 @@ int mrg_set_face_bc(mrg_problem* p, int32_t face, int32_t kind, const double* g)
 /* ---- assembly -------------------------------------------------------------------------------- */
 int mrg_assemble(mrg_problem* p, const double* u_dev, double* r_dev, void* J_vals_dev, uint32_t flags,
                  mrg_stream_t stream);
+/* Residual only: AssemblyManager::assembleRes (assemblyManager_jacres.hpp:669-880), called by the Newton
+ * loop before each Jacobian (solverManager_solvers.hpp:380).  mrg_assemble with MRG_ASM_RES and no J;
+ * flags may add MRG_ASM_OVERWRITE and the path switches (MRG_ASM_JAC and MRG_ASM_J_FP32 are ignored). */
+int mrg_assemble_residual(mrg_problem* p, const double* u_dev, double* r_dev, uint32_t flags, mrg_stream_t stream);
 
 /* ---- linear algebra on the assembled system -------------------------------------------------- */
 /* y = J x on the canonical graph; J_fp32 != 0 means J_vals is float[]. */

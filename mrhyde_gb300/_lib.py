@@ -108,6 +108,7 @@ SIGNATURES = {
     "mrg_set_face_bc": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP]),
     "mrg_set_preconditioner": (C.c_int, [_VP, C.c_int32]),
     "mrg_assemble": (C.c_int, [_VP, _VP, _VP, _VP, C.c_uint32, _VP]),
+    "mrg_assemble_residual": (C.c_int, [_VP, _VP, _VP, C.c_uint32, _VP]),
     "mrg_spmv": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, _VP]),
     "mrg_solve_pcg": (C.c_int, [_VP, _VP, C.c_int32, _VP, _VP, C.c_double, C.c_int32, C.POINTER(SolveStats), _VP]),
     "mrg_newton": (C.c_int, [_VP, _VP, C.POINTER(NewtonOpts), C.POINTER(SolveStats), _VP]),

@@ -250,5 +250,5 @@ class AssemblyManager:
         flags |= L.MRG_ASM_NATIVE_FP64 if native_fp64 else 0
         flags |= (L.MRG_ASM_FORCE_CELL if force_cell else 0) | (L.MRG_ASM_ATOMIC if atomic else 0)
         self._check_args(u, res, None, True, False, False)
-        L.check(L.lib().mrg_assemble(self.problem.handle, _ptr(u), _ptr(res), None, flags, _stream(stream)),
-                "mrg_assemble")
+        L.check(L.lib().mrg_assemble_residual(self.problem.handle, _ptr(u), _ptr(res), flags, _stream(stream)),
+                "mrg_assemble_residual")

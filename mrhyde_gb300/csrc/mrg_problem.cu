@@ -658,3 +658,7 @@ extern "C" int mrg_assemble(mrg_problem* p, const double* u, double* r, void* J,
   if (doJ && (flags & MRG_ASM_FIX_ZERO_ROWS)) return mrg_launch_fix_zero_rows(p, J, fp32, s);
   return MRG_OK;
 }
+
+extern "C" int mrg_assemble_residual(mrg_problem* p, const double* u, double* r, uint32_t flags, mrg_stream_t stream) {
+  return mrg_assemble(p, u, r, nullptr, (flags & ~(uint32_t)(MRG_ASM_JAC | MRG_ASM_J_FP32)) | MRG_ASM_RES, stream);
+}
