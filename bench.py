@@ -783,6 +783,18 @@ def run_profile(args, local_rank):
         torch.cuda.synchronize()
         print(json.dumps({"profile": args.profile, "n": args.general_n, "steps": args.steps, "ok": True}))
         return
+    if args.profile in ("quad64", "quad32"):  # non-affine quadrilaterals, C1 coefficients, stored-geometry path
+        from mrhyde_gb300.workloads import c1_general
+
+        P = Problem(**c1_general(seed=1, n=args.general_quad_n))
+        A = AssemblyManager(P)
+        u = torch.tensor(np.random.default_rng(7).uniform(0.0, 1.0, P.info.n_dofs), device="cuda")
+        r, J = P.new_vector(), P.new_matrix_values(fp32=args.profile == "quad32")
+        for _ in range(args.warmup + args.steps):
+            A.assembleJacRes(u, r, J, fp32_jacobian=args.profile == "quad32", overwrite=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.profile, "n": args.general_quad_n, "steps": args.steps, "ok": True}))
+        return
     if args.profile == "q2tcj":  # the Q2 FP32 Jacobian alone on the tensor cores (coefficients, contraction, rows)
         from mrhyde_gb300.workloads import c3
 
@@ -852,7 +864,7 @@ def main():
                     help="cells per axis of the non-affine quadrilateral leg")
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4",
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4", "quad64", "quad32",
                              "cell64", "cell32", "cellad64", "q2tcj"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
