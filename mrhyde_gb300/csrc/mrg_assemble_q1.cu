@@ -443,8 +443,16 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 7 : 6
     }
   }
   if (DOJ) {
-    __syncthreads();
-    seg_store<JT, !OVW>(J + seg0, sv, seg1 - seg0);
+    if (OVW) {
+      // the staged segment leaves through the copy engine: one bulk copy instead of ~14 16-byte stores
+      // per thread (C2 FP64 0.1612 -> 0.1510 ms, mixed 0.1585 -> 0.1521 ms)
+      mrgdev::fence_to_bulk();
+      __syncthreads();
+      mrgdev::seg_store_bulk<JT>(J + seg0, sv, seg1 - seg0);
+    } else {
+      __syncthreads();
+      seg_store<JT, !OVW>(J + seg0, sv, seg1 - seg0);
+    }
     if (!OVW) {
       __syncthreads();
       if (active && fixed) J[myrow + diagpos] = JT(1);
@@ -568,9 +576,13 @@ __global__ void __launch_bounds__(FT) k_fact_quad(const FactArgs A, const double
     }
   }
   if (DOJ) {
-    __syncthreads();
-    seg_store<JT, !OVW>(J + seg0, sv, seg1 - seg0);
-    if (!OVW) {
+    if (OVW) {
+      mrgdev::fence_to_bulk();
+      __syncthreads();
+      mrgdev::seg_store_bulk<JT>(J + seg0, sv, seg1 - seg0);
+    } else {
+      __syncthreads();
+      seg_store<JT, true>(J + seg0, sv, seg1 - seg0);
       __syncthreads();
       if (active && fixed) J[myrow + diagpos] = JT(1);
     }

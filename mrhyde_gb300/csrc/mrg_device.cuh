@@ -58,6 +58,33 @@ __device__ __forceinline__ void seg_store(T* __restrict__ dst, const T* __restri
   }
 }
 
+// Make this thread's shared-memory writes visible to the bulk-copy (async) proxy; every writing thread
+// executes it before the barrier that precedes seg_store_bulk.
+__device__ __forceinline__ void fence_to_bulk() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Copy a contiguous segment from shared to global memory (overwrite): the 16-byte aligned body with one
+// bulk copy through the copy engine, the ragged ends (at most one 16-byte unit each) with plain stores.
+// src[k] <-> dst[k] share the address phase modulo 16 bytes.  Called by every thread of the CTA after
+// fence_to_bulk and a CTA barrier; thread 0 issues the copy and waits until it has read the shared
+// memory, which must outlive the read (the wait ends as the copy proceeds: it depends on no other CTA).
+template <typename T>
+__device__ __forceinline__ void seg_store_bulk(T* __restrict__ dst, const T* __restrict__ src, int64_t len) {
+  constexpr int V = 16 / sizeof(T);
+  int head = (int)(((16 - ((uintptr_t)dst & 15)) & 15) / sizeof(T));
+  if (head > len) head = (int)len;
+  const int64_t body = (len - head) / V;
+  for (int k = threadIdx.x; k < head; k += blockDim.x) dst[k] = src[k];
+  for (int64_t k = head + body * V + threadIdx.x; k < len; k += blockDim.x) dst[k] = src[k];
+  if (threadIdx.x == 0 && body > 0) {
+    const uint32_t saddr = (uint32_t)__cvta_generic_to_shared(src + head);
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst + head), "r"(saddr),
+                 "r"((uint32_t)(body * 16))
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  }
+}
+
 struct RowInfo {
   int lx, ly, lz, cx, cy, cz;
   int64_t rp;

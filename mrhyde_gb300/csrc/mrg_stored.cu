@@ -360,10 +360,14 @@ __global__ void __launch_bounds__(ST_T, stored_minb<JT, DOJ, DOR>())
   int64_t dglob = 0;
   if (active) row_body<JT, DOJ, DOR, OVW, STAGE>(A, g, n, u, r, sv, seg0, J, fixed, dglob);
   if (STAGE) {
-    __syncthreads();
-    seg_store<JT, !OVW>(J + seg0, sv, seg1 - seg0);
-    if (!OVW) {  // a Dirichlet row's diagonal is replaced, not added to (setJacobianConstraints)
+    if (OVW) {  // the staged segment leaves through the copy engine
+      fence_to_bulk();
       __syncthreads();
+      seg_store_bulk<JT>(J + seg0, sv, seg1 - seg0);
+    } else {
+      __syncthreads();
+      seg_store<JT, true>(J + seg0, sv, seg1 - seg0);
+      __syncthreads();  // a Dirichlet row's diagonal is replaced, not added to (setJacobianConstraints)
       if (active && fixed) J[dglob] = JT(1);
     }
   }
