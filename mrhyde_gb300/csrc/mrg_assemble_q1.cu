@@ -101,11 +101,12 @@ struct FactArgs {
 // SM (80 registers; 0.266 -> 0.253 ms on C2 when introduced; 7 and 8 CTAs, i.e. 72 and 64 registers,
 // spilled more and were slower), FP32 Jacobians 5 (96 registers; 0.252 -> 0.232 ms against the compiler's
 // 117); the interior-row path spills a few words at these floors and is still faster.  Cubic cells (ZAX:
-// sums of scaled conductances, no products) need fewer registers: FP64 7 CTAs (0.1655 -> 0.1640 ms on C2;
-// 8: 0.172 ms), FP32 6 (0.1685 -> 0.1604 ms).  Residual-only instances (no staged row in shared memory):
+// sums of scaled conductances, no products) need fewer registers: FP64 8 CTAs (64 registers, ~100 bytes
+// of spills: 0.1470 -> 0.142 ms on C2 with the bulk segment store; 7: 72 registers), FP32 6 (0.1685 ->
+// 0.1604 ms; 7 within noise, 8 slower).  Residual-only instances (no staged row in shared memory):
 // 8 CTAs per SM, 64 registers with spills, 0.167 -> 0.156 ms on box-cell products (7 CTAs: 0.158 ms).
 template <typename JT, bool DOJ, bool DOR, bool OVW, bool ZAX>
-__global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 7 : 6) : (ZAX ? 6 : 5)))
+__global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 8 : 6) : (ZAX ? 6 : 5)))
     k_fact_hex(const FactArgs A, const double* __restrict__ u, const double* __restrict__ kap,
                const double* __restrict__ kraw, const float* __restrict__ kap32, double* __restrict__ r,
                JT* __restrict__ J) {
