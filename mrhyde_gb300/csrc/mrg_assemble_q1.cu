@@ -146,6 +146,9 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 8 : 6
   const int phase = DOJ ? (int)(((uintptr_t)(J + seg0) & 15) / sizeof(JT)) : 0;
   JT* sv = reinterpret_cast<JT*>(smem_raw) + phase;
 
+  // cubic cells: the scaled conductances come from k_kappa_scale, launched just before this kernel as its
+  // programmatic prerequisite; everything above overlapped its tail, the wait ends when it has completed
+  if constexpr (ZAX) asm volatile("griddepcontrol.wait;" ::: "memory");
   bool fixed = false;
   int64_t diagpos = 0;
   if (active) {
@@ -859,6 +862,7 @@ __global__ void k_kappa32(const double* __restrict__ k, float* __restrict__ k32,
 // entries (one FP64 multiply per cell instead of 21 per row)
 // Two cells per thread with 16-byte accesses (both arrays come from the allocator: 256-byte aligned).
 __global__ void k_kappa_scale(const double* __restrict__ k, double ks, double* __restrict__ out, int64_t n) {
+  asm volatile("griddepcontrol.launch_dependents;");  // the row kernel may be scheduled; it waits for completion
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (2 * i + 1 < n) {
     const double2 v = __ldcs(reinterpret_cast<const double2*>(k) + i);
@@ -884,7 +888,26 @@ cudaError_t launch_fact(const mrg_problem* p, const FactArgs& A, const double* u
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
-    kern<<<grid, FT, smem, s>>>(A, u, scaled ? p->d_kappa_s : p->d_kappa, p->d_kappa, p->d_kappa32, r, J);
+    if (!scaled) {
+      kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa, p->d_kappa32, r, J);
+    } else {
+      // programmatic dependent launch: the row kernel's set-up overlaps the scaling kernel's tail
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(grid);
+      cfg.blockDim = dim3(FT);
+      cfg.dynamicSmemBytes = (size_t)smem;
+      cfg.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      at[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      const double* ks = p->d_kappa_s;
+      const double* kr = p->d_kappa;
+      const float* k32 = p->d_kappa32;
+      const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, A, u, ks, kr, k32, r, J);
+      if (e != cudaSuccess) return e;
+    }
   } else {
     auto kern = k_fact_quad<JT, DOJ, DOR, OVW>;
     kern<<<grid, FT, smem, s>>>(A, u, p->d_kappa, p->d_kappa32, r, J);
