@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(FT, !DOJ ? 8 : (sizeof(JT) == 8 ? (ZAX ? 8 : 6
             if (ZAX && (cls == 1 || cls == 2 || cls == 4)) {
               // K = +0: the product +0 * s is a zero with the sign of s (NaN for a non-finite s), and the
               // residual term -(+-0) * u leaves acc unchanged unless s or u is not finite (then NaN).  No
-              // FP64 instruction: on cubic cells 12 of an interior row's 54.
+              // FP64 instruction for the 6 axis entries of a row.
               const bool sbad = nonfinite(s);
               if (DOJ)
                 sv[loc + pos] = (JT)__longlong_as_double(
