@@ -320,10 +320,91 @@ __device__ __forceinline__ int64_t rowptr_at(const Grid& g, int64_t n, int64_t n
 }
 
 // tab: [G_x | G_y | G_z | Phi] as [q][j] blocks, tab[(d*NL + q)*TS + j], d = 3 for Phi.
+// Q1 1-D tables for the Jacobian: l[q][a] = phi_a(xi_q) at the 2 Gauss points, d[a] = phi_a' (constant)
+struct Tab1 {
+  double l[2][2];
+  double d[2];
+};
+
+// Row l of one Q1 cell's Jacobian, added to acc[0..7] (node and Gauss-point indices x fastest).  The
+// reference gradient of a linear node along its own axis is the constant d[.], so with
+// C(q_b, q_c) = sum over q_a of cw_q the stiffness part along axis a is
+//     s_a^2 d[l_a] d[j_a] sum_{q_b, q_c} C l[q_b][l_b] l[q_c][l_c] l[q_b][j_b] l[q_c][j_c]
+// (two 2 x 2 contractions), and the advective part sum_q b_q phi_j(q) factorises axis by axis: ~200
+// operations per row and cell where the general loop takes ~330.
+template <typename JT>
+__device__ __forceinline__ void q1_cell_row(const Tab1& t1, const JT sq[3], int l, int kind, const JT* __restrict__ tab,
+                                            const JT* __restrict__ qb, JT acc[8]) {
+  constexpr int NL = 8, TS = 8;
+  JT L[2][2], D[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int a = 0; a < 2; ++a) L[q][a] = (JT)t1.l[q][a];
+  D[0] = (JT)t1.d[0];
+  D[1] = (JT)t1.d[1];
+  JT cw[NL];
+#pragma unroll
+  for (int q = 0; q < NL; ++q) cw[q] = qb[q];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+    JT C[2][2] = {{JT(0), JT(0)}, {JT(0), JT(0)}};
+#pragma unroll
+    for (int q = 0; q < NL; ++q) C[(q >> b) & 1][(q >> c) & 1] += cw[q];
+    const int lb = (l >> b) & 1, lc = (l >> c) & 1;
+    JT W[2][2], U[2][2], T[2][2];
+#pragma unroll
+    for (int pb = 0; pb < 2; ++pb)
+#pragma unroll
+      for (int pc = 0; pc < 2; ++pc) W[pb][pc] = C[pb][pc] * L[pb][lb] * L[pc][lc];
+#pragma unroll
+    for (int pb = 0; pb < 2; ++pb)
+#pragma unroll
+      for (int jc = 0; jc < 2; ++jc) U[pb][jc] = W[pb][0] * L[0][jc] + W[pb][1] * L[1][jc];
+#pragma unroll
+    for (int jb = 0; jb < 2; ++jb)
+#pragma unroll
+      for (int jc = 0; jc < 2; ++jc) T[jb][jc] = U[0][jc] * L[0][jb] + U[1][jc] * L[1][jb];
+    const JT f = sq[a] * D[(l >> a) & 1];
+    const JT fd[2] = {f * D[0], f * D[1]};
+#pragma unroll
+    for (int j = 0; j < NL; ++j) acc[j] += fd[(j >> a) & 1] * T[(j >> b) & 1][(j >> c) & 1];
+  }
+  if (kind != MRG_THERMAL) {
+    // b_q = sum_d G_d[q][l] ew_{q,d}, then sum_q b_q phi_j(q) one axis at a time (z, y, then x into acc)
+    JT bq[NL];
+#pragma unroll
+    for (int q = 0; q < NL; ++q)
+      bq[q] = tab[(0 * NL + q) * TS + l] * qb[NL + q] + tab[(1 * NL + q) * TS + l] * qb[2 * NL + q] +
+              tab[(2 * NL + q) * TS + l] * qb[3 * NL + q];
+    JT V1[2][2][2], V2[2][2][2];  // [qx][qy][jz], then [qx][jy][jz]
+#pragma unroll
+    for (int qx = 0; qx < 2; ++qx)
+#pragma unroll
+      for (int qy = 0; qy < 2; ++qy)
+#pragma unroll
+        for (int jz = 0; jz < 2; ++jz)
+          V1[qx][qy][jz] = bq[qx + 2 * qy] * L[0][jz] + bq[qx + 2 * qy + 4] * L[1][jz];
+#pragma unroll
+    for (int qx = 0; qx < 2; ++qx)
+#pragma unroll
+      for (int jy = 0; jy < 2; ++jy)
+#pragma unroll
+        for (int jz = 0; jz < 2; ++jz) V2[qx][jy][jz] = V1[qx][0][jz] * L[0][jy] + V1[qx][1][jz] * L[1][jy];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+      const int jx = j & 1, jy = (j >> 1) & 1, jz = j >> 2;
+      acc[j] += V2[0][jy][jz] * L[0][jx] + V2[1][jy][jz] * L[1][jx];
+    }
+  }
+}
+
 template <int P, typename JT>
 __global__ void __launch_bounds__(JR) k_tp_jac(Grid g, int64_t nrows, int kind, const double s0, const double s1,
                                                const double s2, const JT* __restrict__ tab_g,
-                                               const JT* __restrict__ qbuf, JT* __restrict__ J, int ovw) {
+                                               const JT* __restrict__ qbuf, JT* __restrict__ J, int ovw,
+                                               const Tab1 t1) {
   using K = TP<P>;
   constexpr int N1 = K::N1, NL = K::NL, TS = K::TS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -364,6 +445,9 @@ __global__ void __launch_bounds__(JR) k_tp_jac(Grid g, int64_t nrows, int kind, 
             JT acc[NL];
 #pragma unroll
             for (int j = 0; j < NL; ++j) acc[j] = JT(0);
+            if constexpr (P == 1) {
+              q1_cell_row<JT>(t1, sq, l, kind, tab, qb, acc);
+            } else {
             // stiffness part: alpha_{d,q} = G_d[q][l] s_d^2 cw_q against G_d[q][:]
             for (int q = 0; q < NL; ++q) {
               const JT cw = qb[q];
@@ -384,6 +468,7 @@ __global__ void __launch_bounds__(JR) k_tp_jac(Grid g, int64_t nrows, int kind, 
 #pragma unroll
                 for (int j = 0; j < NL; ++j) acc[j] += b * prow[j];
               }
+            }
             }
             // add into the row: column of local node j of this cell
 #pragma unroll
@@ -557,8 +642,12 @@ static cudaError_t launch_jac_t(mrg_problem* p, const JT* tab, const void* qbuf,
   const int smem = (4 * K::NL * K::TS + JR * K::RMAX + 16 / (int)sizeof(JT)) * (int)sizeof(JT);
   auto kern = k_tp_jac<P, JT>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  Tab1 t1;
+  for (int q = 0; q < 2; ++q)
+    for (int a = 0; a < 2; ++a) t1.l[q][a] = Q->T.phi1[q][a];
+  for (int a = 0; a < 2; ++a) t1.d[a] = Q->T.dph1[0][a];
   kern<<<nblk(p->ndof, JR), JR, smem, s>>>(p->g, p->ndof, p->kind, Q->T.s[0], Q->T.s[1], Q->T.s[2], tab,
-                                           (const JT*)qbuf, J, ovw ? 1 : 0);
+                                           (const JT*)qbuf, J, ovw ? 1 : 0, t1);
   return cudaGetLastError();
 }
 
