@@ -229,13 +229,16 @@ def test_gmg_with_face_terms_matches_oracle(cuda, fp32):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("order,fp32", [(1, False), (2, True)])
-def test_assembly_is_graph_capturable(cuda, order, fp32):
+@pytest.mark.parametrize("order,fp32,n", [(1, False, (6, 5, 4)), (2, True, (6, 5, 4)), (1, False, (6, 6, 6)),
+                                          (1, True, (6, 6, 6))])
+def test_assembly_is_graph_capturable(cuda, order, fp32, n):
     """mrg_assemble enqueues no host synchronisation: after a first call (which may allocate workspace),
-    the call can be captured in a CUDA graph and replaying it reproduces the direct result bit for bit."""
+    the call can be captured in a CUDA graph and replaying it reproduces the direct result bit for bit.
+    Cubic cells (6 x 6 x 6 on the unit cube) capture the scaling kernel and the row kernel launched as its
+    programmatic dependent."""
     from mrhyde_gb300 import AssemblyManager
 
-    cfg = dict(dim=3, order=order, n=(6, 5, 4), kind="thermal" if order == 1 else "diffusion_1pu2",
+    cfg = dict(dim=3, order=order, n=n, kind="thermal" if order == 1 else "diffusion_1pu2",
                dirichlet_faces=1, source=("const", 1.0, 0.0))
     G = gpu_problem(cfg)
     A = AssemblyManager(G)
