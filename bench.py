@@ -780,6 +780,20 @@ def run_profile(args, local_rank):
         torch.cuda.synchronize()
         print(json.dumps({"profile": args.profile, "n": args.general_n, "steps": args.steps, "ok": True}))
         return
+    if args.profile == "q1nl64":  # Q1 1+u^2 FP64 Jacobian + residual on 96^3 box cells (a nonlinear serving request)
+        from mrhyde_gb300 import _lib as LL
+
+        n = 96
+        P = Problem(dim=3, order=1, n=(n, n, n), kind="diffusion_1pu2", source=("const", 10.0, 0.0), kappa=1.0,
+                    dirichlet_faces=LL.MRG_FACE_XLO | LL.MRG_FACE_XHI)
+        A = AssemblyManager(P)
+        u = torch.tensor(np.random.default_rng(3).uniform(0.0, 0.3, P.info.n_dofs), device="cuda")
+        r, J = P.new_vector(), P.new_matrix_values()
+        for _ in range(args.warmup + args.steps):
+            A.assembleJacRes(u, r, J, overwrite=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.profile, "n": n, "steps": args.steps, "ok": True}))
+        return
     if args.profile in ("quad64", "quad32"):  # non-affine quadrilaterals, C1 coefficients, stored-geometry path
         from mrhyde_gb300.workloads import c1_general
 
@@ -861,7 +875,7 @@ def main():
                     help="cells per axis of the non-affine quadrilateral leg")
     ap.add_argument("--c5-count", type=int, default=400)
     ap.add_argument("--c5-slots", type=int, default=12)
-    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4", "quad64", "quad32",
+    ap.add_argument("--profile", default=None, choices=["fp64", "mixed", "residual", "pcg64", "pcg32", "q2tc", "q2cc", "gmg64", "gmg32", "c2newton", "c3gmg", "c4", "quad64", "quad32", "q1nl64",
                              "cell64", "cell32", "cellad64", "q2tcj"],
                     help="run one kernel family only (for ncu captures); prints no bench line")
     args = ap.parse_args()
