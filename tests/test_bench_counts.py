@@ -33,3 +33,20 @@ def _brute(n, hi):
 def test_fp64_instruction_count(n, hi):
     cfg = dict(n=n, lo=(0.0, 0.0, 0.0), hi=hi)
     assert bench.fp64_instructions(cfg) == _brute(n, hi)
+
+
+def test_targets_summary_survives_failed_extras():
+    """The bench line's last key is built from whatever the run produced: extras that failed (an "error"
+    entry) or were skipped leave their targets out instead of breaking the line."""
+    import json
+
+    out = {"ms_per_step": 0.1373, "mixed": {"ms_per_step": 0.142},
+           "roofline": {"frac": 0.67, "fp64_pipe": {"frac": 0.63}}, "e2e": {"value": 8.4e8},
+           "solve": {"error": "RuntimeError: x"}, "c3": {"error": "MrgError: y"}, "general": {},
+           "c4": {"error": "z"}, "c5": {"error": "w"}}
+    t = bench.targets_summary(out)
+    json.dumps(t)
+    assert t["c2_fp64_jacres_ms"] == 0.1373 and t["c2_mixed_jacres_ms"] == 0.142
+    for k in ("c3", "c4", "c5", "general_noaffine"):
+        assert k not in t
+    assert bench.targets_summary({"ms_per_step": 1.0})["c2_fp64_jacres_ms"] == 1.0
